@@ -1,0 +1,624 @@
+// Host side of the GB300 3D FFT backend: plans, engines and the C ABI of
+// include/gbfft.h.
+//
+// An engine is one FFT grid of the reference's multiple-grids API
+// (decomp_2d_fft_engine, src/fft_common.f90:141-242).  At one rank the
+// reference runs, per direction, three batched 1D transforms separated by
+// transposes that are plain copies (src/fft_common_3d.f90, src/fft_cufft.f90:
+// 676-1170).  Here the copies disappear: each axis pass reads its source and
+// writes its destination directly, and the buffers are chosen so that no
+// extra pass and no input-preserving copy (the reference's wk1) is needed:
+//   r2c:  in -> out -> out -> out              (out is the work array)
+//   c2c:  in -> out -> out -> out              (in is never modified)
+//   c2r:  in -> W -> W -> out, W = in when inplace, else the engine's work
+//         area (the complex intermediate does not fit in the real output).
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gbfft.h"
+#include "gbfft_internal.h"
+
+using namespace gbfft;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<int> g_warnings{0};
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return GBFFT_ERR_CUDA;
+}
+
+constexpr unsigned kMagic = 0x47424646u;  // "GBFF"
+
+struct AxisPlan {
+  int n = 1;
+  int nst = 0;
+  int radix[kMaxStages] = {0};
+  int tpl = 1;        // threads per line
+  void* d_tw = nullptr;
+};
+
+// Split n into radix stages: 16s, then one 8/4/2 for the rest of the powers
+// of two, then 3s, 5s, 7s, then any other prime as a generic stage.  Largest
+// radices first.
+bool factorize(int n, AxisPlan& p, std::string& why) {
+  std::vector<int> r;
+  int m = n;
+  int p2 = 0;
+  while (m % 2 == 0) {
+    m /= 2;
+    ++p2;
+  }
+  while (p2 >= 4) {
+    r.push_back(16);
+    p2 -= 4;
+  }
+  if (p2 == 3) r.push_back(8);
+  if (p2 == 2) r.push_back(4);
+  if (p2 == 1) r.push_back(2);
+  for (int q : {7, 5, 3}) {
+    while (m % q == 0) {
+      r.push_back(q);
+      m /= q;
+    }
+  }
+  for (int q = 11; (long long)q * q <= m; q += 2) {
+    while (m % q == 0) {
+      r.push_back(q);
+      m /= q;
+    }
+  }
+  if (m > 1) r.push_back(m);
+  if ((int)r.size() > kMaxStages) {
+    why = "too many radix stages";
+    return false;
+  }
+  p.n = n;
+  p.nst = (int)r.size();
+  for (int i = 0; i < p.nst; ++i) p.radix[i] = r[i];
+  // threads per line: about 8 points per thread, at most one CTA's worth
+  int tpl = (n + 7) / 8;
+  if (tpl > kMaxThreads) tpl = kMaxThreads;
+  if (tpl < 1) tpl = 1;
+  if (n > kMaxN) {
+    why = "axis length " + std::to_string(n) + " exceeds the single-tile limit of " +
+          std::to_string(kMaxN);
+    return false;
+  }
+  p.tpl = tpl;
+  return true;
+}
+
+// Twiddle table exp(-2 pi i m / n), m = 0..n-1, evaluated in long double and
+// rounded once to the working precision.
+std::vector<double> twiddles(int n) {
+  std::vector<double> t(2 * (size_t)n);
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (int m = 0; m < n; ++m) {
+    // reduce to the first half turn for accuracy
+    long double a = two_pi * (long double)m / (long double)n;
+    long double c = cosl(a), s = sinl(a);
+    if (4 * m == n) { c = 0; s = 1; }
+    if (2 * m == n) { c = -1; s = 0; }
+    if (4 * m == 3 * n) { c = 0; s = -1; }
+    t[2 * m] = (double)c;
+    t[2 * m + 1] = (double)(-s);
+  }
+  return t;
+}
+
+int upload_twiddles(AxisPlan& p, int prec) {
+  std::vector<double> t = twiddles(p.n);
+  const size_t bytes = (size_t)p.n * 2 * (size_t)prec;
+  cudaError_t e = cudaMalloc(&p.d_tw, bytes);
+  if (e != cudaSuccess) {
+    p.d_tw = nullptr;
+    return cuda_fail(e, "cudaMalloc(twiddles)");
+  }
+  if (prec == 8) {
+    e = cudaMemcpy(p.d_tw, t.data(), bytes, cudaMemcpyHostToDevice);
+  } else {
+    std::vector<float> f(t.size());
+    for (size_t i = 0; i < t.size(); ++i) f[i] = (float)t[i];
+    e = cudaMemcpy(p.d_tw, f.data(), bytes, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(twiddles)");
+  return GBFFT_OK;
+}
+
+}  // namespace
+
+struct ProfRec {
+  int kind;
+  cudaEvent_t start, stop;
+  double bytes;
+};
+
+struct gbfft_engine_s {
+  unsigned magic = kMagic;
+  bool profiling = false;
+  std::vector<ProfRec> prof;          // launches not yet resolved
+  long long prof_n[GBFFT_PASS_KINDS] = {0};
+  double prof_ms[GBFFT_PASS_KINDS] = {0};
+  double prof_bytes[GBFFT_PASS_KINDS] = {0};
+  int format = GBFFT_PHYSICAL_IN_X;
+  int nx = 0, ny = 0, nz = 0;
+  int inplace = 0;
+  int skip[3] = {0, 0, 0};
+  int prec = 8;
+  int form = GBFFT_FORM_PLAIN;
+  int ph[3] = {0, 0, 0};
+  int sp[3] = {0, 0, 0};
+  AxisPlan ax[3];
+  void* work = nullptr;
+  size_t work_bytes = 0;
+};
+
+namespace {
+
+bool valid_engine(gbfft_engine_t e) { return e != nullptr && e->magic == kMagic; }
+
+void drop_profile(gbfft_engine_t e) {
+  for (auto& r : e->prof) {
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.stop);
+  }
+  e->prof.clear();
+}
+
+void release(gbfft_engine_t e) {
+  drop_profile(e);
+  for (auto& a : e->ax) {
+    if (a.d_tw) cudaFree(a.d_tw);
+    a.d_tw = nullptr;
+  }
+  if (e->work) cudaFree(e->work);
+  e->work = nullptr;
+}
+
+size_t cbytes(const gbfft_engine_s* e) { return 2 * (size_t)e->prec; }
+
+// Lines per CTA for a pass with the given plan.
+int lines_per_cta(const AxisPlan& p, int prec, bool contiguous, long long nlines, int* tpl_out) {
+  int tpl = p.tpl;
+  int L;
+  if (contiguous) {
+    L = 256 / tpl;
+    if (L < 1) L = 1;
+  } else {
+    // a warp row should cover at least 64 contiguous bytes of x
+    const int min_l = (int)(64 / (2 * prec));
+    L = 512 / tpl;
+    if (L > 32) L = 32;
+    if (L < min_l) L = min_l;
+    while (L * tpl > kMaxThreads && tpl > 32) tpl /= 2;
+    while (L > 1 && L * tpl > kMaxThreads) L /= 2;
+  }
+  while (L > 1 && pass_smem_bytes(prec, p.n, L) > 100 * 1024) L /= 2;
+  *tpl_out = tpl;
+  if (L > 1 && nlines < L) {
+    int l2 = 1;
+    while (l2 < nlines) l2 *= 2;
+    L = l2;
+  }
+  return L < 1 ? 1 : L;
+}
+
+// Fill the plan-dependent fields of a pass.
+void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind) {
+  a.n = p.n;
+  a.nst = p.nst;
+  for (int i = 0; i < kMaxStages; ++i) a.radix[i] = i < p.nst ? p.radix[i] : 0;
+  a.tw = p.d_tw;
+  a.L = lines_per_cta(p, prec, contiguous, a.nlines, &a.tpl);
+  a.first_fused = 0;
+  a.last_fused = 0;
+  (void)kind;
+}
+
+struct Pass {
+  PassArgs a;
+  int kind;
+  bool contiguous;
+  int prof_kind;   // GBFFT_PASS_*
+  double bytes;    // algorithmic bytes: one read + one write of the array
+};
+
+// c2c along `axis` of a complex (n1, n2, n3) array.
+Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const void* src, void* dst,
+              int inverse) {
+  Pass P;
+  PassArgs& a = P.a;
+  std::memset(&a, 0, sizeof(a));
+  a.src = src;
+  a.dst = dst;
+  a.inverse = inverse;
+  P.kind = K_C2C;
+  if (axis == 0) {
+    P.contiguous = true;
+    a.s_src_n = a.s_dst_n = 1;
+    a.s_src_l = a.s_dst_l = n1;
+    a.nlines = n2 * n3;
+    a.nv = 1;
+  } else if (axis == 1) {
+    P.contiguous = false;
+    a.s_src_n = a.s_dst_n = n1;
+    a.s_src_l = a.s_dst_l = (long long)n1 * n2;
+    a.nlines = n1;
+    a.nv = n3;
+  } else {
+    P.contiguous = false;
+    a.s_src_n = a.s_dst_n = (long long)n1 * n2;
+    a.s_src_l = a.s_dst_l = n1;
+    a.nlines = n1;
+    a.nv = n2;
+  }
+  fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C);
+  P.prof_kind = GBFFT_PASS_C2C_X + axis;
+  P.bytes = 2.0 * (double)n1 * n2 * n3 * (double)cbytes(e);
+  return P;
+}
+
+// r2c (kind K_R2C) or c2r (K_C2R) along the engine's real axis.
+Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst) {
+  Pass P;
+  PassArgs& a = P.a;
+  std::memset(&a, 0, sizeof(a));
+  a.src = src;
+  a.dst = dst;
+  P.kind = kind;
+  const int nx = e->nx, ny = e->ny, nz = e->nz;
+  long long real_s_n, real_s_l, cplx_s_n, cplx_s_l;
+  if (e->format == GBFFT_PHYSICAL_IN_X) {
+    P.contiguous = true;
+    real_s_n = cplx_s_n = 1;
+    real_s_l = nx;
+    cplx_s_l = nx / 2 + 1;
+    a.real_lines = ny * nz;
+    a.nv = 1;
+  } else {
+    P.contiguous = false;
+    real_s_n = cplx_s_n = (long long)nx * ny;
+    real_s_l = cplx_s_l = nx;
+    a.real_lines = nx;
+    a.nv = ny;
+  }
+  a.nlines = (a.real_lines + 1) / 2;
+  if (kind == K_R2C) {
+    a.s_src_n = real_s_n;
+    a.s_src_l = real_s_l;
+    a.s_dst_n = cplx_s_n;
+    a.s_dst_l = cplx_s_l;
+    a.inverse = 0;
+  } else {
+    a.s_src_n = cplx_s_n;
+    a.s_src_l = cplx_s_l;
+    a.s_dst_n = real_s_n;
+    a.s_dst_l = real_s_l;
+    a.inverse = 1;
+  }
+  const int axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
+  fill_plan(a, e->ax[axis], e->prec, P.contiguous, kind);
+  P.prof_kind = kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R;
+  P.bytes = (double)nx * ny * nz * e->prec +
+            (double)e->sp[0] * e->sp[1] * e->sp[2] * (double)cbytes(e);
+  return P;
+}
+
+int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st) {
+  for (const Pass& p : ps) {
+    if (!p.contiguous && p.a.nv > 65535)
+      return fail(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
+    ProfRec rec{p.prof_kind, nullptr, nullptr, p.bytes};
+    if (e->profiling) {
+      if (cudaEventCreate(&rec.start) != cudaSuccess || cudaEventCreate(&rec.stop) != cudaSuccess)
+        return fail(GBFFT_ERR_CUDA, "cudaEventCreate");
+      cudaEventRecord(rec.start, st);
+    }
+    cudaError_t err = launch_axis_pass(e->prec, p.kind, p.contiguous, p.a, st);
+    if (e->profiling) {
+      cudaEventRecord(rec.stop, st);
+      e->prof.push_back(rec);
+    }
+    if (err != cudaSuccess) return cuda_fail(err, "axis pass launch");
+  }
+  return GBFFT_OK;
+}
+
+bool overlap(const void* a, size_t na, const void* b, size_t nb) {
+  const char* pa = (const char*)a;
+  const char* pb = (const char*)b;
+  return pa < pb + nb && pb < pa + na;
+}
+
+void warn_skip(int code) {
+  g_warnings.fetch_add(1);
+  std::fprintf(stderr, "gbfft warning %d: r2c / c2r transform can not be skipped\n", code);
+}
+
+}  // namespace
+
+int gbfft::set_error(int code, const char* msg) {
+  g_err = msg ? msg : "";
+  return code;
+}
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* gbfft_last_error_string(void) { return g_err.c_str(); }
+
+int gbfft_warning_count(void) { return g_warnings.load(); }
+
+int gbfft_version(int* major, int* minor) {
+  if (major) *major = 0;
+  if (minor) *minor = 1;
+  return GBFFT_OK;
+}
+
+long long gbfft_launch_count(void) { return launch_counter(); }
+
+int gbfft_malloc(void** d_ptr, size_t bytes) {
+  if (!d_ptr) return fail(GBFFT_ERR_INVALID, "gbfft_malloc: null output pointer");
+  *d_ptr = nullptr;
+  if (bytes == 0) return GBFFT_OK;
+  cudaError_t e = cudaMalloc(d_ptr, bytes);
+  if (e != cudaSuccess) {
+    *d_ptr = nullptr;
+    g_err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return GBFFT_ERR_ALLOC;
+  }
+  return GBFFT_OK;
+}
+
+int gbfft_free(void* d_ptr) {
+  if (!d_ptr) return GBFFT_OK;
+  cudaError_t e = cudaFree(d_ptr);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFree");
+  return GBFFT_OK;
+}
+
+int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const int* skip, int prec,
+                        int form, gbfft_engine_t* engine) {
+  if (!engine) return fail(GBFFT_ERR_INVALID, "engine output pointer is null");
+  *engine = nullptr;
+  // same checks and order as src/fft_common.f90:157-166, :210-216
+  if (nx <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for nx");
+  if (ny <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for ny");
+  if (nz <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for nz");
+  if (format != GBFFT_PHYSICAL_IN_X && format != GBFFT_PHYSICAL_IN_Z)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for pencil");
+  if (prec != GBFFT_PREC_SINGLE && prec != GBFFT_PREC_DOUBLE)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for precision (4 or 8)");
+  if (form != GBFFT_FORM_PLAIN && form != GBFFT_FORM_SPLIT)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for form");
+  if (form == GBFFT_FORM_SPLIT)
+    return fail(GBFFT_ERR_UNSUPPORTED, "split tensor-core form is not available in this build");
+  const long long cells = (long long)nx * ny * nz;
+  if (cells > (1LL << 40)) return fail(GBFFT_ERR_UNSUPPORTED, "grid too large");
+  if ((long long)ny * nz > 0x7fffffffLL || (long long)nx * ny > 0x7fffffffLL)
+    return fail(GBFFT_ERR_UNSUPPORTED, "line count exceeds 2^31");
+
+  gbfft_engine_s* e = new (std::nothrow) gbfft_engine_s();
+  if (!e) return fail(GBFFT_ERR_ALLOC, "host allocation failed");
+  e->format = format;
+  e->nx = nx;
+  e->ny = ny;
+  e->nz = nz;
+  e->inplace = inplace ? 1 : 0;
+  for (int i = 0; i < 3; ++i) e->skip[i] = skip ? (skip[i] ? 1 : 0) : 0;
+  e->prec = prec;
+  e->form = form;
+  e->ph[0] = nx;
+  e->ph[1] = ny;
+  e->ph[2] = nz;
+  e->sp[0] = format == GBFFT_PHYSICAL_IN_X ? nx / 2 + 1 : nx;
+  e->sp[1] = ny;
+  e->sp[2] = format == GBFFT_PHYSICAL_IN_Z ? nz / 2 + 1 : nz;
+
+  const int lens[3] = {nx, ny, nz};
+  for (int d = 0; d < 3; ++d) {
+    std::string why;
+    if (!factorize(lens[d], e->ax[d], why)) {
+      delete e;
+      return fail(GBFFT_ERR_UNSUPPORTED, why);
+    }
+    if (pass_smem_bytes(prec, lens[d], 1) > 200 * 1024) {
+      delete e;
+      return fail(GBFFT_ERR_UNSUPPORTED, "axis length " + std::to_string(lens[d]) +
+                                             " does not fit one shared-memory tile at this precision");
+    }
+    int rc = upload_twiddles(e->ax[d], prec);
+    if (rc != GBFFT_OK) {
+      release(e);
+      delete e;
+      return rc;
+    }
+  }
+  // c2r work area: the complex intermediate, unless the input may be used
+  if (!e->inplace) {
+    e->work_bytes = (size_t)e->sp[0] * e->sp[1] * e->sp[2] * cbytes(e);
+    cudaError_t err = cudaMalloc(&e->work, e->work_bytes);
+    if (err != cudaSuccess) {
+      e->work = nullptr;
+      release(e);
+      delete e;
+      g_err = std::string("cudaMalloc(work area): ") + cudaGetErrorString(err);
+      return GBFFT_ERR_ALLOC;
+    }
+  }
+  *engine = e;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_destroy(gbfft_engine_t e) {
+  if (!e) return GBFFT_OK;
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  release(e);
+  e->magic = 0;
+  delete e;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_get_sizes(gbfft_engine_t e, int ph[3], int sp[3]) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  for (int i = 0; i < 3; ++i) {
+    if (ph) ph[i] = e->ph[i];
+    if (sp) sp[i] = e->sp[i];
+  }
+  return GBFFT_OK;
+}
+
+int gbfft_engine_work_bytes(gbfft_engine_t e, size_t* bytes) {
+  if (!valid_engine(e) || !bytes) return fail(GBFFT_ERR_INVALID, "bad argument");
+  *bytes = e->work_bytes;
+  return GBFFT_OK;
+}
+
+int gbfft_exec_r2c(gbfft_engine_t e, const void* d_in, void* d_out, void* stream) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (!d_in || !d_out) return fail(GBFFT_ERR_INVALID, "null array pointer");
+  const size_t rb = (size_t)e->nx * e->ny * e->nz * e->prec;
+  const size_t cb = (size_t)e->sp[0] * e->sp[1] * e->sp[2] * cbytes(e);
+  if (overlap(d_in, rb, d_out, cb))
+    return fail(GBFFT_ERR_INVALID, "In-place r2c transform is not yet available");
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<Pass> ps;
+  const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
+  if (e->format == GBFFT_PHYSICAL_IN_X) {
+    if (e->skip[0]) warn_skip(1);
+    ps.push_back(real_pass(e, K_R2C, d_in, d_out));
+    if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
+    if (!e->skip[2]) ps.push_back(c2c_pass(e, 2, s1, s2, s3, d_out, d_out, 0));
+  } else {
+    if (e->skip[2]) warn_skip(2);
+    ps.push_back(real_pass(e, K_R2C, d_in, d_out));
+    if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
+    if (!e->skip[0]) ps.push_back(c2c_pass(e, 0, s1, s2, s3, d_out, d_out, 0));
+  }
+  return run_passes(e, ps, st);
+}
+
+int gbfft_exec_c2r(gbfft_engine_t e, void* d_in, void* d_out, void* stream) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (!d_in || !d_out) return fail(GBFFT_ERR_INVALID, "null array pointer");
+  const size_t rb = (size_t)e->nx * e->ny * e->nz * e->prec;
+  const size_t cb = (size_t)e->sp[0] * e->sp[1] * e->sp[2] * cbytes(e);
+  if (overlap(d_in, cb, d_out, rb))
+    return fail(GBFFT_ERR_INVALID, "In-place c2r transform is not yet available");
+  cudaStream_t st = (cudaStream_t)stream;
+  void* W = e->inplace ? d_in : e->work;
+  if (!W) return fail(GBFFT_ERR_STATE, "engine has no work area");
+  const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
+  std::vector<Pass> ps;
+  const void* cur = d_in;
+  // c2c passes in the reference's order (src/fft_common_3d.f90:216-283)
+  const int order_x[2] = {2, 1};  // PHYSICAL_IN_X: z then y, then c2r along x
+  const int order_z[2] = {0, 1};  // PHYSICAL_IN_Z: x then y, then c2r along z
+  const int* order = e->format == GBFFT_PHYSICAL_IN_X ? order_x : order_z;
+  for (int i = 0; i < 2; ++i) {
+    const int ax = order[i];
+    if (e->skip[ax]) continue;
+    ps.push_back(c2c_pass(e, ax, s1, s2, s3, cur, W, 1));
+    cur = W;
+  }
+  if (e->format == GBFFT_PHYSICAL_IN_X && e->skip[0]) warn_skip(3);
+  if (e->format == GBFFT_PHYSICAL_IN_Z && e->skip[2]) warn_skip(4);
+  ps.push_back(real_pass(e, K_C2R, cur, d_out));
+  return run_passes(e, ps, st);
+}
+
+int gbfft_exec_c2c(gbfft_engine_t e, void* d_in, void* d_out, int isign, void* stream) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (!d_in || !d_out) return fail(GBFFT_ERR_INVALID, "null array pointer");
+  if (isign != GBFFT_FORWARD && isign != GBFFT_BACKWARD)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for isign");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n1 = e->nx, n2 = e->ny, n3 = e->nz;
+  const size_t bytes = (size_t)n1 * n2 * n3 * cbytes(e);
+  if (d_in != d_out && overlap(d_in, bytes, d_out, bytes))
+    return fail(GBFFT_ERR_INVALID, "input and output partially overlap");
+  const bool x_first = (e->format == GBFFT_PHYSICAL_IN_X && isign == GBFFT_FORWARD) ||
+                       (e->format == GBFFT_PHYSICAL_IN_Z && isign == GBFFT_BACKWARD);
+  const int order_f[3] = {0, 1, 2}, order_b[3] = {2, 1, 0};
+  const int* order = x_first ? order_f : order_b;
+  const int inv = isign == GBFFT_BACKWARD ? 1 : 0;
+  std::vector<Pass> ps;
+  const void* cur = d_in;
+  for (int i = 0; i < 3; ++i) {
+    const int ax = order[i];
+    if (e->skip[ax]) continue;
+    ps.push_back(c2c_pass(e, ax, n1, n2, n3, cur, d_out, inv));
+    cur = d_out;
+  }
+  if (ps.empty()) {
+    cudaError_t err = launch_copy(d_in, d_out, bytes, st);
+    if (err != cudaSuccess) return cuda_fail(err, "copy launch");
+    return GBFFT_OK;
+  }
+  return run_passes(e, ps, st);
+}
+
+int gbfft_transpose(int kind, int is_complex, int prec, const void* d_src, void* d_dst, int n1, int n2,
+                    int n3, void* stream) {
+  if (kind < GBFFT_X_TO_Y || kind > GBFFT_Y_TO_X) return fail(GBFFT_ERR_INVALID, "Invalid transpose kind");
+  if (prec != GBFFT_PREC_SINGLE && prec != GBFFT_PREC_DOUBLE)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for precision (4 or 8)");
+  if (n1 < 0 || n2 < 0 || n3 < 0) return fail(GBFFT_ERR_INVALID, "negative size");
+  const size_t bytes = (size_t)n1 * n2 * n3 * (size_t)prec * (is_complex ? 2 : 1);
+  if (bytes == 0) return GBFFT_OK;
+  if (!d_src || !d_dst) return fail(GBFFT_ERR_INVALID, "null array pointer");
+  if (d_src != d_dst && overlap(d_src, bytes, d_dst, bytes))
+    return fail(GBFFT_ERR_INVALID, "source and destination partially overlap");
+  cudaError_t err = launch_copy(d_src, d_dst, bytes, (cudaStream_t)stream);
+  if (err != cudaSuccess) return cuda_fail(err, "transpose copy launch");
+  return GBFFT_OK;
+}
+
+int gbfft_engine_set_profiling(gbfft_engine_t e, int enable) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  drop_profile(e);
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k) {
+    e->prof_n[k] = 0;
+    e->prof_ms[k] = 0;
+    e->prof_bytes[k] = 0;
+  }
+  e->profiling = enable != 0;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_profile_read(gbfft_engine_t e, int kind, long long* launches, double* ms,
+                              double* bytes) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (kind < 0 || kind >= GBFFT_PASS_KINDS) return fail(GBFFT_ERR_INVALID, "bad pass kind");
+  for (auto& r : e->prof) {
+    cudaError_t err = cudaEventSynchronize(r.stop);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaEventSynchronize");
+    float t = 0;
+    cudaEventElapsedTime(&t, r.start, r.stop);
+    e->prof_n[r.kind] += 1;
+    e->prof_ms[r.kind] += t;
+    e->prof_bytes[r.kind] += r.bytes;
+  }
+  drop_profile(e);
+  if (launches) *launches = e->prof_n[kind];
+  if (ms) *ms = e->prof_ms[kind];
+  if (bytes) *bytes = e->prof_bytes[kind];
+  return GBFFT_OK;
+}
+
+}  // extern "C"

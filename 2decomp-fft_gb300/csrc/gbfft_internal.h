@@ -1,0 +1,78 @@
+// Internal declarations shared by the kernels and the host engine of the
+// GB300 3D FFT backend.  Nothing here is part of the C ABI (include/gbfft.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace gbfft {
+
+constexpr int kMaxStages = 16;    // radix stages of one axis plan
+constexpr int kMaxE = 16;         // complex values a thread holds in one stage
+constexpr int kMaxThreads = 512;  // threads in one CTA of an axis pass
+constexpr int kMaxN = 8192;       // longest axis a single-tile pass supports
+
+// What one axis pass does to each line.
+enum Kind : int {
+  K_C2C = 0,  // complex line -> complex line
+  K_R2C = 1,  // two real lines -> two half spectra (n/2+1 values each)
+  K_C2R = 2,  // two half spectra -> two real lines
+};
+
+// Radices with a hand-written butterfly; any other factor runs through the
+// generic direct-sum stage.
+__host__ __device__ constexpr bool radix_is_special(int r) {
+  return r == 2 || r == 3 || r == 4 || r == 5 || r == 7 || r == 8 || r == 16;
+}
+
+// Arguments of one batched-line FFT pass along one axis of a 3D array.
+//
+// A "line" is one 1D transform.  Two addressings exist:
+//   contiguous (the x axis): line l starts at l * s_l, point n at + n * s_n;
+//   strided   (the y and z axes): lines are indexed by (u, v) with u the
+//     x index (unit stride, so a warp reads neighbouring lines in one
+//     transaction) and v the remaining axis; line (u, v) starts at
+//     u + v * s_l and point n sits at + n * s_n.
+// For K_R2C / K_C2R two neighbouring real lines (2c, 2c+1 along l or u) are
+// carried by one complex line c.  All strides are in elements of the
+// array's own type (real elements for the real side of r2c/c2r).
+struct PassArgs {
+  const void* src;
+  void* dst;
+  const void* tw;  // n complex roots exp(-2 pi i m / n), m = 0..n-1
+  long long s_src_n, s_src_l;
+  long long s_dst_n, s_dst_l;
+  int n;           // transform length
+  int nst;         // number of radix stages (0 when n == 1)
+  int L;           // complex lines per CTA
+  int tpl;         // threads per line
+  int inverse;     // 1: backward (+i) transform, done as conj(F(conj(x)))
+  int nlines;      // complex lines along l (contiguous) or u (strided)
+  int real_lines;  // r2c/c2r: real lines along l or u (may be odd)
+  int nv;          // strided: extent of v (grid.y)
+  int first_fused; // stage 0 reads global memory directly
+  int last_fused;  // last stage writes global memory directly
+  int radix[kMaxStages];
+};
+
+// Shared memory a pass needs for L lines of length n (padded layout).
+size_t pass_smem_bytes(int prec_bytes, int n, int L);
+
+// Enqueue one axis pass.  prec_bytes = 4 (float) or 8 (double).
+cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous,
+                             const PassArgs& a, cudaStream_t stream);
+
+// Enqueue an identity-layout copy of `bytes` bytes (the one-rank transpose).
+cudaError_t launch_copy(const void* src, void* dst, size_t bytes,
+                        cudaStream_t stream);
+
+// Record an error message for gbfft_last_error_string(); returns `code`.
+int set_error(int code, const char* msg);
+
+// Count of kernels this library has enqueued (for the benchmark's report).
+long long launch_counter();
+void add_launches(long long n);
+
+}  // namespace gbfft

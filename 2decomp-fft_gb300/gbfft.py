@@ -1,0 +1,373 @@
+"""ctypes front end of libgbfft.so (include/gbfft.h, include/decomp_2d_fft.h).
+
+This is a thin binding used by the tests and the benchmark: every call goes
+through the C ABI, with device arrays passed as raw pointers.  torch is used
+only to own device memory and streams.  There is no CPU path here: when the
+library is missing the import fails loudly.
+
+Array convention: a reference pencil ``a(nx, ny, nz)`` (x fastest) is a
+C-contiguous tensor of shape ``(nz, ny, nx)``.  Spectral arrays of r2c/c2r are
+``(nz, ny, nx//2+1)`` (PHYSICAL_IN_X) or ``(nz//2+1, ny, nx)``
+(PHYSICAL_IN_Z), of dtype complex64 (single) or complex128 (double).
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libgbfft.so")
+
+OK = 0
+ERR_INVALID = 1
+ERR_ALLOC = 2
+ERR_CUDA = 3
+ERR_UNSUPPORTED = 4
+ERR_STATE = 5
+ERR_TIMEOUT = 6
+
+PHYSICAL_IN_X = 1
+PHYSICAL_IN_Z = 3
+FORWARD = -1
+BACKWARD = 1
+PREC_SINGLE = 4
+PREC_DOUBLE = 8
+FORM_PLAIN = 0
+FORM_SPLIT = 1
+X_TO_Y, Y_TO_Z, Z_TO_Y, Y_TO_X = 0, 1, 2, 3
+PASS_NAMES = ["r2c", "c2r", "c2c_x", "c2c_y", "c2c_z"]
+D2D_FFT_BACKEND = 5
+
+# Every symbol the two public headers declare, with (restype, argtypes).
+_vp, _i, _ip, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_size_t
+SIGNATURES = {
+    "gbfft_engine_create": (_i, [_i, _i, _i, _i, _i, _ip, _i, _i, ctypes.POINTER(_vp)]),
+    "gbfft_engine_destroy": (_i, [_vp]),
+    "gbfft_engine_get_sizes": (_i, [_vp, _ip, _ip]),
+    "gbfft_engine_work_bytes": (_i, [_vp, ctypes.POINTER(_sz)]),
+    "gbfft_exec_r2c": (_i, [_vp, _vp, _vp, _vp]),
+    "gbfft_exec_c2r": (_i, [_vp, _vp, _vp, _vp]),
+    "gbfft_exec_c2c": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "gbfft_transpose": (_i, [_i, _i, _i, _vp, _vp, _i, _i, _i, _vp]),
+    "gbfft_malloc": (_i, [ctypes.POINTER(_vp), _sz]),
+    "gbfft_free": (_i, [_vp]),
+    "gbfft_last_error_string": (ctypes.c_char_p, []),
+    "gbfft_warning_count": (_i, []),
+    "gbfft_batch_create": (_i, [ctypes.POINTER(_vp)]),
+    "gbfft_batch_add": (_i, [_vp, _vp, _vp, _vp]),
+    "gbfft_batch_forward": (_i, [_vp, _vp]),
+    "gbfft_batch_backward": (_i, [_vp, _vp]),
+    "gbfft_batch_graph_build": (_i, [_vp, _vp]),
+    "gbfft_batch_graph_launch": (_i, [_vp, _vp]),
+    "gbfft_batch_destroy": (_i, [_vp]),
+    "gbfft_engine_set_profiling": (_i, [_vp, _i]),
+    "gbfft_engine_profile_read": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_longlong),
+                                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "gbfft_version": (_i, [_ip, _ip]),
+    "gbfft_launch_count": (ctypes.c_longlong, []),
+    # decomp_2d_fft.h
+    "d2d_decomp_2d_init": (_i, [_i, _i, _i, _i, _i, _i]),
+    "d2d_decomp_2d_finalize": (_i, []),
+    "d2d_get_decomp_main": (_i, [_ip] * 9),
+    "d2d_transpose_x_to_y": (_i, [_vp, _vp, _i]),
+    "d2d_transpose_y_to_z": (_i, [_vp, _vp, _i]),
+    "d2d_transpose_z_to_y": (_i, [_vp, _vp, _i]),
+    "d2d_transpose_y_to_x": (_i, [_vp, _vp, _i]),
+    "d2d_fft_set_default_inplace": (_i, [_i]),
+    "d2d_fft_init": (_i, [_i, _i, _i, _i, _i, _i, _i, _i, _ip]),
+    "d2d_fft_set_ngrid": (_i, [_i]),
+    "d2d_fft_get_ngrid": (_i, []),
+    "d2d_fft_use_grid": (_i, [_i]),
+    "d2d_fft_get_engine": (_i, [_i, ctypes.POINTER(_vp)]),
+    "d2d_fft_3d_c2c": (_i, [_vp, _vp, _i]),
+    "d2d_fft_3d_r2c": (_i, [_vp, _vp]),
+    "d2d_fft_3d_c2r": (_i, [_vp, _vp]),
+    "d2d_fft_finalize": (_i, []),
+    "d2d_fft_get_size": (_i, [_ip, _ip, _ip]),
+    "d2d_fft_get_ph_size": (_i, [_ip]),
+    "d2d_fft_get_sp_size": (_i, [_ip]),
+    "d2d_fft_get_format": (_i, []),
+    "d2d_fft_get_inplace": (_i, []),
+    "d2d_fft_get_inplace_r2c": (_i, []),
+    "d2d_fft_get_inplace_c2r": (_i, []),
+    "d2d_fft_backend": (_i, []),
+    "d2d_set_stream": (_i, [_vp]),
+    "d2d_fft_log": (_i, [ctypes.c_char_p, _i]),
+}
+
+
+class GbfftError(RuntimeError):
+    """A nonzero status from the library, with its message."""
+
+    def __init__(self, status, message):
+        super().__init__("gbfft status %d: %s" % (status, message))
+        self.status = status
+        self.message = message
+
+
+_lib = None
+
+
+def lib():
+    """Load libgbfft.so (built by __graft_entry__.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libgbfft.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error():
+    return lib().gbfft_last_error_string().decode()
+
+
+def check(status):
+    if status != OK:
+        raise GbfftError(status, last_error())
+    return status
+
+
+def launch_count():
+    return int(lib().gbfft_launch_count())
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return ctypes.c_void_p(stream)
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _int3(x):
+    return (ctypes.c_int * 3)(*[int(v) for v in x])
+
+
+def spectral_shape(nx, ny, nz, fmt):
+    if fmt == PHYSICAL_IN_X:
+        return (nz, ny, nx // 2 + 1)
+    return (nz // 2 + 1, ny, nx)
+
+
+class Engine:
+    """One FFT grid (gbfft_engine_create / destroy)."""
+
+    def __init__(self, fmt, nx, ny, nz, inplace=False, skip=None, prec=PREC_DOUBLE,
+                 form=FORM_PLAIN):
+        self.h = ctypes.c_void_p()
+        sk = _int3([int(bool(s)) for s in skip]) if skip is not None else None
+        check(lib().gbfft_engine_create(int(fmt), int(nx), int(ny), int(nz), int(bool(inplace)),
+                                        sk, int(prec), int(form), ctypes.byref(self.h)))
+        self.fmt, self.nx, self.ny, self.nz = fmt, nx, ny, nz
+        self.prec, self.inplace = prec, inplace
+
+    def close(self):
+        if self.h:
+            check(lib().gbfft_engine_destroy(self.h))
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sizes(self):
+        ph, sp = (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+        check(lib().gbfft_engine_get_sizes(self.h, ph, sp))
+        return tuple(ph), tuple(sp)
+
+    def work_bytes(self):
+        b = ctypes.c_size_t()
+        check(lib().gbfft_engine_work_bytes(self.h, ctypes.byref(b)))
+        return b.value
+
+    def r2c(self, x, out, stream=None):
+        check(lib().gbfft_exec_r2c(self.h, _ptr(x), _ptr(out), _stream(stream)))
+        return out
+
+    def c2r(self, x, out, stream=None):
+        check(lib().gbfft_exec_c2r(self.h, _ptr(x), _ptr(out), _stream(stream)))
+        return out
+
+    def c2c(self, x, out, isign, stream=None):
+        check(lib().gbfft_exec_c2c(self.h, _ptr(x), _ptr(out), int(isign), _stream(stream)))
+        return out
+
+    def set_profiling(self, enable):
+        check(lib().gbfft_engine_set_profiling(self.h, int(bool(enable))))
+
+    def profile(self):
+        """{pass name: (launches, total ms, total algorithmic bytes)}"""
+        res = {}
+        for k, name in enumerate(PASS_NAMES):
+            n, ms, by = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+            check(lib().gbfft_engine_profile_read(self.h, k, ctypes.byref(n), ctypes.byref(ms),
+                                                  ctypes.byref(by)))
+            if n.value:
+                res[name] = (n.value, ms.value, by.value)
+        return res
+
+    # torch conveniences ------------------------------------------------
+    def _dtypes(self):
+        import torch
+        return (torch.float64, torch.complex128) if self.prec == PREC_DOUBLE else (torch.float32, torch.complex64)
+
+    def empty_spectral(self, device="cuda"):
+        import torch
+        return torch.empty(spectral_shape(self.nx, self.ny, self.nz, self.fmt),
+                           dtype=self._dtypes()[1], device=device)
+
+    def empty_physical(self, complex_=False, device="cuda"):
+        import torch
+        return torch.empty((self.nz, self.ny, self.nx), dtype=self._dtypes()[1 if complex_ else 0],
+                           device=device)
+
+
+def transpose(kind, src, dst, n1, n2, n3, is_complex, prec, stream=None):
+    check(lib().gbfft_transpose(int(kind), int(bool(is_complex)), int(prec), _ptr(src), _ptr(dst),
+                                int(n1), int(n2), int(n3), _stream(stream)))
+    return dst
+
+
+class Batch:
+    """gbfft_batch_*: independent grids run as one batch / one CUDA graph."""
+
+    def __init__(self):
+        self.h = ctypes.c_void_p()
+        check(lib().gbfft_batch_create(ctypes.byref(self.h)))
+        self._keep = []
+
+    def add(self, engine, real, spec):
+        check(lib().gbfft_batch_add(self.h, engine.h, _ptr(real), _ptr(spec)))
+        self._keep.append((engine, real, spec))
+
+    def forward(self, stream=None):
+        check(lib().gbfft_batch_forward(self.h, _stream(stream)))
+
+    def backward(self, stream=None):
+        check(lib().gbfft_batch_backward(self.h, _stream(stream)))
+
+    def graph_build(self, stream):
+        check(lib().gbfft_batch_graph_build(self.h, _stream(stream)))
+
+    def graph_launch(self, stream=None):
+        check(lib().gbfft_batch_graph_launch(self.h, _stream(stream)))
+
+    def close(self):
+        if self.h:
+            check(lib().gbfft_batch_destroy(self.h))
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# Mirror of the reference module API (decomp_2d_fft.h)
+# ---------------------------------------------------------------------------
+def decomp_2d_init(nx, ny, nz, p_row=0, p_col=0, prec=PREC_DOUBLE):
+    check(lib().d2d_decomp_2d_init(nx, ny, nz, p_row, p_col, prec))
+
+
+def decomp_2d_finalize():
+    check(lib().d2d_decomp_2d_finalize())
+
+
+def decomp_main():
+    arrs = [(ctypes.c_int * 3)() for _ in range(9)]
+    check(lib().d2d_get_decomp_main(*arrs))
+    keys = ["xst", "xen", "xsz", "yst", "yen", "ysz", "zst", "zen", "zsz"]
+    return {k: tuple(a) for k, a in zip(keys, arrs)}
+
+
+def transpose_x_to_y(src, dst, is_complex=False):
+    check(lib().d2d_transpose_x_to_y(_ptr(src), _ptr(dst), int(bool(is_complex))))
+
+
+def transpose_y_to_z(src, dst, is_complex=False):
+    check(lib().d2d_transpose_y_to_z(_ptr(src), _ptr(dst), int(bool(is_complex))))
+
+
+def transpose_z_to_y(src, dst, is_complex=False):
+    check(lib().d2d_transpose_z_to_y(_ptr(src), _ptr(dst), int(bool(is_complex))))
+
+
+def transpose_y_to_x(src, dst, is_complex=False):
+    check(lib().d2d_transpose_y_to_x(_ptr(src), _ptr(dst), int(bool(is_complex))))
+
+
+def decomp_2d_fft_init(pencil=PHYSICAL_IN_X, nx=0, ny=0, nz=0, igrid=0, opt_inplace=None,
+                       opt_inplace_r2c=None, opt_inplace_c2r=None, opt_skip_XYZ_c2c=None):
+    sk = _int3([int(bool(s)) for s in opt_skip_XYZ_c2c]) if opt_skip_XYZ_c2c is not None else None
+    opt = lambda v: -1 if v is None else int(bool(v))
+    check(lib().d2d_fft_init(pencil, nx, ny, nz, igrid, opt(opt_inplace), opt(opt_inplace_r2c),
+                             opt(opt_inplace_c2r), sk))
+
+
+def decomp_2d_fft_set_ngrid(n):
+    check(lib().d2d_fft_set_ngrid(n))
+
+
+def decomp_2d_fft_get_ngrid():
+    return lib().d2d_fft_get_ngrid()
+
+
+def decomp_2d_fft_use_grid(igrid=0):
+    check(lib().d2d_fft_use_grid(igrid))
+
+
+def decomp_2d_fft_3d_c2c(x, out, isign):
+    check(lib().d2d_fft_3d_c2c(_ptr(x), _ptr(out), int(isign)))
+
+
+def decomp_2d_fft_3d_r2c(x, out):
+    check(lib().d2d_fft_3d_r2c(_ptr(x), _ptr(out)))
+
+
+def decomp_2d_fft_3d_c2r(x, out):
+    check(lib().d2d_fft_3d_c2r(_ptr(x), _ptr(out)))
+
+
+def decomp_2d_fft_finalize():
+    check(lib().d2d_fft_finalize())
+
+
+def decomp_2d_fft_get_size():
+    a, b, c = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+    check(lib().d2d_fft_get_size(a, b, c))
+    return tuple(a), tuple(b), tuple(c)
+
+
+def decomp_2d_fft_get_ph_size():
+    a = (ctypes.c_int * 3)()
+    check(lib().d2d_fft_get_ph_size(a))
+    return tuple(a)
+
+
+def decomp_2d_fft_get_sp_size():
+    a = (ctypes.c_int * 3)()
+    check(lib().d2d_fft_get_sp_size(a))
+    return tuple(a)
+
+
+def set_stream(stream):
+    check(lib().d2d_set_stream(_stream(stream) if stream is not None else None))
+
+
+def decomp_2d_fft_log():
+    buf = ctypes.create_string_buffer(1024)
+    check(lib().d2d_fft_log(buf, 1024))
+    return buf.value.decode()

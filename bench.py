@@ -1,0 +1,501 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 3D FFT backend on its headline workload.
+
+Default workload: 3D r2c forward then c2r backward on a 1024 x 1024 x 512
+real FP32 grid (PHYSICAL_IN_X), one step = one round trip.  The metric is
+GPts/s = nx*ny*nz / t(r2c + c2r), summed over ranks (each rank runs its own
+grid: replicas, no data-path collective).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+  python bench.py --impl reference ...   (the reference's CPU path)
+
+`value` is measured with the input already resident in HBM (CUDA events on
+the launching stream, K steps between a barrier + synchronize on both
+sides, max over ranks).  `e2e` is the same metric through the C ABI with
+host buffers: every step copies the input from pinned host memory, runs
+r2c + c2r, and copies the result back.  Inputs (2 GiB real + 2.1 GiB
+spectral) are larger than the 129 MB L2, so no flush is needed between
+steps.  The CPU leg times the oracle -- the restated generic backend of the
+reference -- on a bounded sample of the same line passes and scales it to
+the full grid.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "2decomp-fft_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "3D r2c+c2r GPts/s & %HBM roofline; split-TC vs plain FP32 at rel-L2≤1e-6"
+
+WORKLOADS = {
+    # name: (nx, ny, nz, format, precision, input kind)
+    "r2c_c2r_1024x1024x512_f32_x": (1024, 1024, 512, 1, 4, "gauss_modes"),
+    "r2c_c2r_1024x1024x512_f32_z": (1024, 1024, 512, 3, 4, "gauss_modes"),
+    "r2c_c2r_64x64x64_f64_x": (64, 64, 64, 1, 8, "uniform"),
+    "r2c_c2r_384x400x243_f64_x": (384, 400, 243, 1, 8, "uniform"),
+    "r2c_c2r_384x400x243_f32_x": (384, 400, 243, 1, 4, "uniform"),
+    "r2c_c2r_360x270x210_f64_x": (360, 270, 210, 1, 8, "uniform"),
+    "r2c_c2r_360x270x210_f32_x": (360, 270, 210, 1, 4, "uniform"),
+    "r2c_c2r_256x256x256_f32_x": (256, 256, 256, 1, 4, "uniform"),
+}
+DEFAULT_WORKLOAD = "r2c_c2r_1024x1024x512_f32_x"
+
+
+# ---------------------------------------------------------------------------
+# ranks
+# ---------------------------------------------------------------------------
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _dist():
+    try:
+        import torch.distributed as dist
+        return dist if dist.is_available() and dist.is_initialized() else None
+    except Exception:
+        return None
+
+
+def barrier():
+    d = _dist()
+    if d is not None:
+        d.barrier()
+
+
+def max_over_ranks(x):
+    """Largest value of x over all ranks (the step time the job sees)."""
+    d = _dist()
+    if d is None:
+        return float(x)
+    import torch
+    dev = "cuda" if d.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    d.all_reduce(t, op=d.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x):
+    d = _dist()
+    if d is None:
+        return float(x)
+    import torch
+    dev = "cuda" if d.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    d.all_reduce(t, op=d.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self, t0, t1):
+        rows = []
+        for ts, line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            rows.append((ts, parts))
+        inside = [r for r in rows if t0 - 0.15 <= r[0] <= t1 + 0.15] or rows
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+
+        def num(v):
+            try:
+                return float(v)
+            except Exception:
+                return None
+
+        sm = sorted(x for x in (num(p[1]) for _, p in inside) if x is not None)
+        smax = max((x for x in (num(p[2]) for _, p in inside) if x is not None), default=None)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for _, p in inside:
+            for name, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        pw = [x for x in (num(p[3]) for _, p in inside) if x is not None]
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(inside),
+                "power_w_max": max(pw) if pw else None}
+
+
+# ---------------------------------------------------------------------------
+# inputs
+# ---------------------------------------------------------------------------
+def make_input(nx, ny, nz, kind, dtype, device):
+    """Seeded synthetic field of the workload's shape (nz, ny, nx)."""
+    import torch
+    if kind == "gauss_modes":
+        # N(0, 1) noise (seed 3) plus 8 modes 10 sin(2 pi (kx x/nx + ky y/ny
+        # + kz z/nz) + phi), k uniform in 1..8 per axis, phi uniform (seed 4)
+        g = torch.Generator(device=device).manual_seed(3)
+        x = torch.randn((nz, ny, nx), generator=g, device=device, dtype=torch.float32)
+        import numpy as np
+        rng = np.random.default_rng(4)
+        xs = torch.arange(nx, device=device, dtype=torch.float64) / nx
+        ys = torch.arange(ny, device=device, dtype=torch.float64) / ny
+        zs = torch.arange(nz, device=device, dtype=torch.float64) / nz
+        for _ in range(8):
+            kx, ky, kz = (int(v) for v in rng.integers(1, 9, size=3))
+            phi = float(rng.uniform(0, 2 * np.pi))
+            arg = (2 * np.pi * (kx * xs[None, None, :] + ky * ys[None, :, None] + kz * zs[:, None, None]) + phi)
+            x += (10.0 * torch.sin(arg)).to(torch.float32)
+        return x.to(dtype).contiguous()
+    g = torch.Generator(device=device).manual_seed(5)
+    return (torch.rand((nz, ny, nx), generator=g, device=device, dtype=torch.float64) * 2 - 1).to(dtype)
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle on a bounded sample of the same line passes
+# ---------------------------------------------------------------------------
+def cpu_sample(nx, ny, nz, fmt, prec, seconds_target=12.0, threads=None):
+    """Time the generic backend's six line passes of one r2c + c2r round trip
+    on a bounded subset of each pass's lines (the full-size arrays, real
+    strides), and scale each pass to its full line count.  Returns
+    (estimated GPts/s, threads, description)."""
+    import numpy as np
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    O.set_threads(threads)
+    p = "d" if prec == 8 else "s"
+    rt, ct = (np.float64, np.complex128) if prec == 8 else (np.float32, np.complex64)
+    real = np.full((nz, ny, nx), 0.5, dtype=rt)
+    if fmt == 1:
+        s1, s2, s3 = nx // 2 + 1, ny, nz
+        passes = [("r2c", 0, ny * nz), ("c2c", 1, s1 * s3), ("c2c", 2, s1 * s2),
+                  ("c2c", 2, s1 * s2), ("c2c", 1, s1 * s3), ("c2r", 0, ny * nz)]
+    else:
+        s1, s2, s3 = nx, ny, nz // 2 + 1
+        passes = [("r2c", 2, nx * ny), ("c2c", 1, s1 * s3), ("c2c", 0, s2 * s3),
+                  ("c2c", 0, s2 * s3), ("c2c", 1, s1 * s3), ("c2r", 2, nx * ny)]
+    spec = np.full((s3, s2, s1), 0.25 + 0.5j, dtype=ct)
+
+    def run(kind, axis, lines):
+        if kind == "r2c":
+            O.sample_pass("r2c", axis, real, spec, nx, ny, nz, lines, p)
+        elif kind == "c2r":
+            O.sample_pass("c2r", axis, spec, real, nx, ny, nz, lines, p)
+        else:
+            O.sample_pass("c2c", axis, spec, None, s1, s2, s3, lines, p)
+
+    per_pass = seconds_target / len(passes)
+    total_est = 0.0
+    sampled = []
+    for kind, axis, total_lines in passes:
+        probe = min(total_lines, 4 * threads)
+        t = time.perf_counter()
+        run(kind, axis, probe)
+        dt = max(time.perf_counter() - t, 1e-6)
+        lines = int(min(total_lines, max(probe, probe * per_pass / dt)))
+        t = time.perf_counter()
+        run(kind, axis, lines)
+        dt = time.perf_counter() - t
+        total_est += dt * total_lines / lines
+        sampled.append("%s-%s %d/%d lines" % (kind, "xyz"[axis], lines, total_lines))
+    gpts = nx * ny * nz / total_est / 1e9
+    desc = ("oracle (restated generic backend, Glassman FFT, %s) on the first lines of each of the "
+            "6 line passes of one r2c+c2r round trip over the full-size arrays, scaled to all lines: %s"
+            % ("double" if prec == 8 else "single", "; ".join(sampled)))
+    return gpts, threads, desc, total_est
+
+
+# ---------------------------------------------------------------------------
+# accuracy against FP64
+# ---------------------------------------------------------------------------
+def fp64_accuracy(x_dev, spec_dev, fmt):
+    import numpy as np
+    try:
+        import scipy.fft as sfft
+        kw = {"workers": os.cpu_count() or 1}
+    except Exception:
+        sfft, kw = np.fft, {}
+    x = x_dev.cpu().numpy().astype(np.float64)
+    if fmt == 1:
+        ref = sfft.rfftn(x, axes=(0, 1, 2), **kw)
+    else:
+        ref = sfft.rfftn(x, axes=(2, 1, 0), **kw)
+    got = spec_dev.cpu().numpy()
+    d = got.astype(np.complex128) - ref
+    rel = float(np.linalg.norm(d) / np.linalg.norm(ref))
+    mx = float(np.abs(d).max() / np.abs(ref).max())
+    return rel, mx
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+    import gbfft
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    nx, ny, nz, fmt, prec, kind = WORKLOADS[args.workload]
+    rdt = torch.float32 if prec == 4 else torch.float64
+    gbfft.lib()
+
+    eng = gbfft.Engine(fmt, nx, ny, nz, prec=prec)
+    x = make_input(nx, ny, nz, kind, rdt, dev)
+    spec = eng.empty_spectral(device=dev)
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream(dev)
+    npts = nx * ny * nz
+
+    def step():
+        eng.r2c(x, spec, stream)
+        eng.c2r(spec, y, stream)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    l0 = gbfft.launch_count()
+    t_wall0 = time.time()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    barrier()
+    launches = gbfft.launch_count() - l0
+    ms = e0.elapsed_time(e1) / args.steps
+    ms_max = max_over_ranks(ms)
+    total_pts = sum_over_ranks(npts)
+    value = total_pts / (ms_max * 1e-3) / 1e9
+
+    # per-pass device times (events around each pass on the same stream)
+    eng.set_profiling(True)
+    prof_steps = max(3, min(args.steps, 10))
+    for _ in range(prof_steps):
+        step()
+    torch.cuda.synchronize()
+    prof = eng.profile()
+    eng.set_profiling(False)
+    clocks.stop()
+    clk = clocks.summary(t_wall0, t_wall1)
+
+    passes = {}
+    for name, (n, tms, by) in prof.items():
+        passes[name] = {"launches_per_step": n / prof_steps, "ms_per_launch": tms / n,
+                        "gbs": by / (tms * 1e-3) / 1e9, "bytes_per_launch": by / n}
+    dom = max(prof.items(), key=lambda kv: kv[1][1])[0] if prof else None
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if peak else "fallback 6800 GB/s"
+    peak = peak or 6800.0
+    algo_bytes_step = sum(v[2] for v in prof.values()) / prof_steps if prof else None
+    roof = None
+    if dom:
+        d = passes[dom]
+        roof = {"bound": "hbm", "kernel": "axis pass %s" % dom, "achieved": round(d["gbs"], 1),
+                "peak": peak, "unit": "GB/s", "frac": round(d["gbs"] / peak, 4),
+                "traffic": read_traffic(args.workload, dom), "peak_source": peak_src,
+                "step_frac": round(algo_bytes_step / (ms_max * 1e-3) / 1e9 / peak, 4)}
+
+    # end to end through the C ABI with host buffers
+    xh = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+    xh.copy_(x)
+    yh = torch.empty_like(xh, pin_memory=True)
+    xd = torch.empty_like(x)
+    e2e_steps = max(3, min(args.steps, 20))
+
+    def e2e_step():
+        xd.copy_(xh, non_blocking=True)
+        eng.r2c(xd, spec, stream)
+        eng.c2r(spec, y, stream)
+        yh.copy_(y, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps)
+    e2e = {"value": round(total_pts / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GPts/s",
+           "ms_per_step": round(e2e_ms, 3),
+           "h2d_bytes_per_step": x.numel() * x.element_size(),
+           "d2h_bytes_per_step": y.numel() * y.element_size()}
+
+    out = None
+    if rank == 0:
+        acc = {}
+        if not args.no_accuracy:
+            step()
+            torch.cuda.synchronize()
+            rel, mx = fp64_accuracy(x, spec, fmt)
+            yy = (y.double() / npts - x.double())
+            rt = float(torch.linalg.vector_norm(yy) / torch.linalg.vector_norm(x.double()))
+            acc = {"rel_l2_vs_fp64": rel, "max_abs_rel_vs_fp64": mx, "round_trip_rel_l2": rt,
+                   "fp64_reference": "pocketfft (scipy.fft) FP64 on the same input"}
+        cpu = None
+        if not args.no_cpu:
+            g, thr, desc, est = cpu_sample(nx, ny, nz, fmt, prec, seconds_target=args.cpu_seconds)
+            cpu = {"value": round(g, 5), "unit": "GPts/s", "cores": thr, "kind": "port",
+                   "sample": desc, "est_seconds_full_round_trip": round(est, 2)}
+        out = {
+            "metric": METRIC,
+            "value": round(value, 3),
+            "unit": "GPts/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms_max, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32" if prec == 4 else "f64",
+            "data": "synthetic: %s" % ("seeded N(0,1) + 8 sinusoid modes of amplitude 10" if kind == "gauss_modes"
+                                       else "seeded uniform [-1,1)"),
+            "config": {"workload": "r2c+c2r round trip %dx%dx%d %s %s" % (
+                nx, ny, nz, "fp32" if prec == 4 else "fp64", "PHYSICAL_IN_X" if fmt == 1 else "PHYSICAL_IN_Z"),
+                "name": args.workload, "nx": nx, "ny": ny, "nz": nz, "form": "plain",
+                "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas (one grid per GPU)"},
+            "roofline": roof,
+            "passes": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                       for k, v in passes.items()},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "accuracy": acc,
+        }
+        print(json.dumps(out), flush=True)
+    eng.close()
+    d = _dist()
+    if d is not None:
+        d.destroy_process_group()
+    return out
+
+
+def read_traffic(workload, kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/dram_traffic.txt: `workload kernel bytes_per_launch`)."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 3 and not line.startswith("#") and parts[0] == workload and parts[1] == kernel:
+                return float(parts[2])
+    except Exception:
+        pass
+    return None
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return None
+    nx, ny, nz, fmt, prec, kind = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.ref_step_seconds)
+    vals = []
+    desc = ""
+    for i in range(args.warmup + args.steps):
+        g, thr, desc, est = cpu_sample(nx, ny, nz, fmt, prec, seconds_target=per_step, threads=threads)
+        if i >= args.warmup:
+            vals.append(g)
+    v = sum(vals) / len(vals)
+    out = {"metric": METRIC, "value": round(v, 5), "unit": "GPts/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(nx * ny * nz / (v * 1e9) * 1e3, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32" if prec == 4 else "f64", "data": "synthetic (constant-valued arrays; the "
+           "line FFT cost does not depend on the values)", "impl": "reference",
+           "config": {"workload": "r2c+c2r round trip %dx%dx%d %s %s" % (
+               nx, ny, nz, "fp32" if prec == 4 else "fp64", "PHYSICAL_IN_X" if fmt == 1 else "PHYSICAL_IN_Z"),
+               "name": args.workload, "nx": nx, "ny": ny, "nz": nz,
+               "parallelism": "OpenMP threads over lines on the host cores"},
+           "cpu_baseline": {"value": round(v, 5), "unit": "GPts/s", "cores": threads, "kind": "port",
+                            "sample": desc},
+           "e2e": {"value": round(v, 5), "unit": "GPts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=3.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

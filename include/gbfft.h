@@ -1,0 +1,165 @@
+/*
+ * gbfft.h -- C ABI of the GB300 (sm_103a) 3D FFT backend for 2DECOMP&FFT at
+ * one rank (p_row = p_col = 1).
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns an int status (GBFFT_OK = 0).  On failure the message is available
+ * from gbfft_last_error_string() (thread-local).  Device pointers are CUDA
+ * device addresses; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * Calls are stream-ordered: they enqueue work and return without waiting,
+ * exactly like the cuFFT exec calls they replace.
+ *
+ * Array layout: a 3D array (n1, n2, n3) is stored with the first index
+ * fastest (Fortran order), as every 2DECOMP pencil is.  Complex values are
+ * interleaved (re, im).  At one rank the X-, Y- and Z-pencil of a field share
+ * the same shape and the same layout.
+ */
+#ifndef GBFFT_H
+#define GBFFT_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define GBFFT_OK 0
+#define GBFFT_ERR_INVALID 1     /* bad argument (size, format, pointer)      */
+#define GBFFT_ERR_ALLOC 2       /* device allocation failed                  */
+#define GBFFT_ERR_CUDA 3        /* a CUDA runtime call failed                */
+#define GBFFT_ERR_UNSUPPORTED 4 /* valid request this backend cannot run     */
+#define GBFFT_ERR_STATE 5       /* wrong call order (use before init, ...)   */
+#define GBFFT_ERR_TIMEOUT 6     /* a bounded device wait gave up             */
+
+/* ---- constants, same values as src/decomp_2d_constants.f90 ----------- */
+#define GBFFT_PHYSICAL_IN_X 1 /* decomp_2d_constants.f90:92 PHYSICAL_IN_X */
+#define GBFFT_PHYSICAL_IN_Z 3 /* decomp_2d_constants.f90:93 PHYSICAL_IN_Z */
+#define GBFFT_FORWARD (-1)    /* decomp_2d_constants.f90:86 DECOMP_2D_FFT_FORWARD */
+#define GBFFT_BACKWARD 1      /* decomp_2d_constants.f90:87 DECOMP_2D_FFT_BACKWARD */
+#define GBFFT_D2D_FFT_BACKEND 5 /* new id beside D2D_FFT_BACKEND_CUFFT = 4 (:81) */
+
+/* precision of an engine: mytype of the reference build (DOUBLE_PREC or not) */
+#define GBFFT_PREC_SINGLE 4
+#define GBFFT_PREC_DOUBLE 8
+
+/* arithmetic form of the axis passes */
+#define GBFFT_FORM_PLAIN 0 /* CUDA-core FP32 / FP64 butterflies              */
+#define GBFFT_FORM_SPLIT 1 /* radix-16 stages as split-FP16 tensor-core DFTs  */
+
+/* transpose kinds (src/decomp_2d.f90:140-222 generic transpose_* names) */
+#define GBFFT_X_TO_Y 0
+#define GBFFT_Y_TO_Z 1
+#define GBFFT_Z_TO_Y 2
+#define GBFFT_Y_TO_X 3
+
+typedef struct gbfft_engine_s* gbfft_engine_t;
+
+/* Create one FFT grid.  Replaces decomp_2d_fft_engine_init + init_fft_engine
+ * of the cuFFT backend (src/fft_common.f90:141-242, src/fft_cufft.f90:263-431):
+ * validates sizes and format with the same rules, builds the per-axis plans
+ * and twiddle tables, and allocates the work area.
+ *   format  GBFFT_PHYSICAL_IN_X or GBFFT_PHYSICAL_IN_Z
+ *   inplace nonzero = OVERWRITE: c2c/c2r may destroy their input
+ *   skip    NULL or three flags: skip the x / y / z c2c transforms
+ *           (opt_skip_XYZ_c2c; r2c/c2r along the real axis cannot be skipped
+ *           and only warns, as src/fft_generic.f90:221-222 does)
+ *   prec    GBFFT_PREC_SINGLE or GBFFT_PREC_DOUBLE
+ *   form    GBFFT_FORM_PLAIN or GBFFT_FORM_SPLIT (SPLIT needs PREC_SINGLE) */
+int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace,
+                        const int* skip, int prec, int form,
+                        gbfft_engine_t* engine);
+
+/* Free plans, tables and work area (src/fft_cufft.f90:436-470,
+ * finalize_fft_engine). */
+int gbfft_engine_destroy(gbfft_engine_t engine);
+
+/* Sizes of the physical (ph) and spectral (sp) arrays, (n1, n2, n3) each:
+ * decomp_2d_fft_get_size / ph%xsz / sp%xsz at one rank
+ * (src/fft_common.f90:204-216, :311-327). */
+int gbfft_engine_get_sizes(gbfft_engine_t engine, int ph[3], int sp[3]);
+
+/* Bytes of device work area the engine holds (0 when none is needed). */
+int gbfft_engine_work_bytes(gbfft_engine_t engine, size_t* bytes);
+
+/* 3D r2c, forward, unnormalised: fft_3d_r2c (src/fft_common_3d.f90:121-189,
+ * GPU src/fft_cufft.f90:795-934).  d_in real ph-shaped, d_out complex
+ * sp-shaped.  d_in is not modified.  d_in and d_out must not overlap. */
+int gbfft_exec_r2c(gbfft_engine_t engine, const void* d_in, void* d_out,
+                   void* stream);
+
+/* 3D c2r, backward, unnormalised: fft_3d_c2r (src/fft_common_3d.f90:194-296,
+ * GPU src/fft_cufft.f90:939-1170).  d_in complex sp-shaped is preserved
+ * unless the engine is inplace. */
+int gbfft_exec_c2r(gbfft_engine_t engine, void* d_in, void* d_out,
+                   void* stream);
+
+/* 3D c2c: fft_3d_c2c (src/fft_common_3d.f90:9-116, GPU src/fft_cufft.f90:676-790).
+ * isign = GBFFT_FORWARD or GBFFT_BACKWARD.  d_in == d_out is allowed. */
+int gbfft_exec_c2c(gbfft_engine_t engine, void* d_in, void* d_out, int isign,
+                   void* stream);
+
+/* transpose_x_to_y / y_to_z / z_to_y / y_to_x at one rank: an identity-layout
+ * copy of n1*n2*n3 elements (src/transpose_x_to_y.f90:41-50,
+ * src/transpose_y_to_z.f90:40-49, src/transpose_z_to_y.f90:41-47,
+ * src/transpose_y_to_x.f90:41).  is_complex selects complex(mytype). */
+int gbfft_transpose(int kind, int is_complex, int prec, const void* d_src,
+                    void* d_dst, int n1, int n2, int n3, void* stream);
+
+/* Device memory for pencil arrays: replaces alloc_x/alloc_y/alloc_z of the
+ * device build (src/alloc_dev.f90:10-135).  gbfft_malloc returns 256-byte
+ * aligned memory. */
+int gbfft_malloc(void** d_ptr, size_t bytes);
+int gbfft_free(void* d_ptr);
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char* gbfft_last_error_string(void);
+
+/* Number of warnings raised so far ("r2c / c2r transform can not be
+ * skipped", src/fft_generic.f90:221-222), for callers that check them. */
+int gbfft_warning_count(void);
+
+/* ---- batched uneven grids (the multiple-grids use of
+ *      src/fft_common.f90:381-479) ------------------------------------- */
+typedef struct gbfft_batch_s* gbfft_batch_t;
+
+/* A batch groups engines of the same precision and plain form.  Each item
+ * is one engine with its own input and output; gbfft_batch_forward runs every
+ * item's r2c, gbfft_batch_backward every item's c2r. */
+int gbfft_batch_create(gbfft_batch_t* batch);
+int gbfft_batch_add(gbfft_batch_t batch, gbfft_engine_t engine,
+                    const void* d_real, void* d_spec);
+int gbfft_batch_forward(gbfft_batch_t batch, void* stream);
+int gbfft_batch_backward(gbfft_batch_t batch, void* stream);
+/* Capture forward then backward of the whole batch in one CUDA graph and
+ * replay it: gbfft_batch_graph_launch enqueues the replay on `stream`. */
+int gbfft_batch_graph_build(gbfft_batch_t batch, void* stream);
+int gbfft_batch_graph_launch(gbfft_batch_t batch, void* stream);
+int gbfft_batch_destroy(gbfft_batch_t batch);
+
+/* ---- per-pass device timing, for benchmarks ---------------------------
+ * While enabled, every axis pass an engine enqueues is bracketed by two CUDA
+ * events recorded on the pass's stream.  gbfft_engine_profile_read resolves
+ * them (it waits for the events) and returns, for pass kind `kind`
+ * (GBFFT_PASS_*), the number of launches, their summed device time in ms and
+ * the summed algorithmic bytes (one read and one write of the array). */
+#define GBFFT_PASS_R2C 0
+#define GBFFT_PASS_C2R 1
+#define GBFFT_PASS_C2C_X 2
+#define GBFFT_PASS_C2C_Y 3
+#define GBFFT_PASS_C2C_Z 4
+#define GBFFT_PASS_KINDS 5
+int gbfft_engine_set_profiling(gbfft_engine_t engine, int enable);
+int gbfft_engine_profile_read(gbfft_engine_t engine, int kind, long long* launches,
+                              double* ms, double* bytes);
+
+/* Library version and kernel-launch counter (every kernel this library has
+ * enqueued since load), for benchmarks that report launches. */
+int gbfft_version(int* major, int* minor);
+long long gbfft_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFFT_H */
