@@ -61,6 +61,7 @@ SIGNATURES = {
     "gbfft_engine_set_profiling": (_i, [_vp, _i]),
     "gbfft_engine_profile_read": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "gbfft_exec_c2r_noalloc": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp]),
     "gbfft_version": (_i, [_ip, _ip]),
     "gbfft_launch_count": (ctypes.c_longlong, []),
     # decomp_2d_fft.h
@@ -231,6 +232,16 @@ class Engine:
         import torch
         return torch.empty((self.nz, self.ny, self.nx), dtype=self._dtypes()[1 if complex_ else 0],
                            device=device)
+
+
+NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024
+
+
+def c2r_noalloc(fmt, nx, ny, nz, prec, x, out, stream=None):
+    """gbfft_exec_c2r_noalloc: c2r that allocates no device memory."""
+    check(lib().gbfft_exec_c2r_noalloc(int(fmt), int(nx), int(ny), int(nz), int(prec), _ptr(x),
+                                       _ptr(out), _stream(stream)))
+    return out
 
 
 def transpose(kind, src, dst, n1, n2, n3, is_complex, prec, stream=None):

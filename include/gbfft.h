@@ -153,6 +153,25 @@ int gbfft_engine_set_profiling(gbfft_engine_t engine, int enable);
 int gbfft_engine_profile_read(gbfft_engine_t engine, int kind, long long* launches,
                               double* ms, double* bytes);
 
+/* ---- allocation-free c2r ---------------------------------------------
+ * No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory (code running under another runtime's memory
+ * pool, inside a callback, or after reserving all device memory up front).
+ * It does what gbfft_exec_c2r does for a non-OVERWRITE engine without skip
+ * flags (input preserved, unnormalised), but takes the grid description
+ * instead of an engine and allocates nothing: its twiddle tables and its
+ * work area live in one static device array of GBFFT_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading this library holds until the process exits.
+ *   - Sizes whose tables + spectral-sized work area exceed the array are
+ *     rejected with GBFFT_ERR_INVALID.
+ *   - All calls share the array: calls whose GPU work overlaps (other
+ *     streams, other host threads) race and corrupt each other.
+ *   - The first call on a device (with it current) looks up the array's
+ *     device address; make that first call before any stream capture. */
+#define GBFFT_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int gbfft_exec_c2r_noalloc(int format, int nx, int ny, int nz, int prec,
+                           const void* d_in, void* d_out, void* stream);
+
 /* Library version and kernel-launch counter (every kernel this library has
  * enqueued since load), for benchmarks that report launches. */
 int gbfft_version(int* major, int* minor);
