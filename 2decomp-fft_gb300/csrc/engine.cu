@@ -216,8 +216,45 @@ int lines_per_cta(const AxisPlan& p, int prec, bool contiguous, long long nlines
   return L < 1 ? 1 : L;
 }
 
+// Lines per CTA for the power-of-two kernel (n / 16 threads per line).
+int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines) {
+  const int tpl = n / 16;
+  const int maxt = prec == 4 ? kFastMaxThreadsF32 : kFastMaxThreadsF64;
+  int L;
+  if (contiguous) {
+    L = 256 / tpl;
+  } else {
+    const int min_l = (int)(64 / (2 * prec));
+    L = 512 / tpl;
+    if (L > 32) L = 32;
+    if (L < min_l) L = min_l;
+  }
+  while (L > 1 && L * tpl > maxt) L /= 2;
+  const size_t line_bytes = (size_t)n * 2 * prec;
+  while (L > 1 && (size_t)L * line_bytes > 96 * 1024) L /= 2;
+  if (L < 1) L = 1;
+  if (L > 1 && nlines < L) {
+    int l2 = 1;
+    while (l2 < nlines) l2 *= 2;
+    L = l2;
+  }
+  return L;
+}
+
 // Fill the plan-dependent fields of a pass.
 void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind) {
+  if (fast_length(p.n)) {
+    a.n = p.n;
+    a.nst = 0;
+    a.tw = p.d_tw;
+    a.fast = 1;
+    a.tpl = p.n / 16;
+    a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines);
+    a.first_fused = 1;
+    a.last_fused = kind != K_R2C;
+    (void)kind;
+    return;
+  }
   a.n = p.n;
   a.nst = p.nst;
   for (int i = 0; i < kMaxStages; ++i) a.radix[i] = i < p.nst ? p.radix[i] : 0;

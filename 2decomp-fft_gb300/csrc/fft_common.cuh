@@ -1,0 +1,284 @@
+// Complex helpers, radix butterflies and the per-line addressing shared by
+// the axis-pass kernels (fft_axis.cu: runtime plans; fft_fast.cu:
+// compile-time power-of-two plans).
+#pragma once
+
+#include "gbfft_internal.h"
+
+namespace gbfft {
+namespace dev {
+
+template <typename T> struct CxOf;
+template <> struct CxOf<float> { using type = float2; };
+template <> struct CxOf<double> { using type = double2; };
+template <typename T> using Cx = typename CxOf<T>::type;
+
+template <typename C> __device__ __forceinline__ C cmk(decltype(C::x) a, decltype(C::x) b) {
+  C r;
+  r.x = a;
+  r.y = b;
+  return r;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return cmk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return cmk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  return cmk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * (-i)
+template <typename C> __device__ __forceinline__ C cmul_mi(C a) { return cmk<C>(a.y, -a.x); }
+
+// ---------------------------------------------------------------------------
+// Forward butterflies (sign -1), natural order in and out.
+// ---------------------------------------------------------------------------
+template <typename C> __device__ __forceinline__ void dft4v(C& a0, C& a1, C& a2, C& a3) {
+  C t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = cmul_mi(csub(a1, a3));
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = cadd(t1, t3);
+  a3 = csub(t1, t3);
+}
+
+template <typename C> __device__ __forceinline__ void dft2p(C* v) {
+  C a = v[0];
+  v[0] = cadd(a, v[1]);
+  v[1] = csub(a, v[1]);
+}
+
+template <typename C> __device__ __forceinline__ void dft4p(C* v) { dft4v(v[0], v[1], v[2], v[3]); }
+
+template <typename C> __device__ __forceinline__ void dft3p(C* v) {
+  using T = decltype(C::x);
+  const T h = T(-0.5), s = T(0.86602540378443864676);
+  C t = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+  C m = cmk<C>(v[0].x + h * t.x, v[0].y + h * t.y);
+  v[0] = cadd(v[0], t);
+  v[1] = cmk<C>(m.x + s * d.y, m.y - s * d.x);
+  v[2] = cmk<C>(m.x - s * d.y, m.y + s * d.x);
+}
+
+template <typename C> __device__ __forceinline__ void dft5p(C* v) {
+  using T = decltype(C::x);
+  const T c1 = T(0.3090169943749474241), c2 = T(-0.8090169943749474241);
+  const T s1 = T(0.95105651629515357212), s2 = T(0.58778525229247312917);
+  C t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+  C t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+  C a0 = v[0];
+  C m1 = cmk<C>(a0.x + c1 * t1.x + c2 * t2.x, a0.y + c1 * t1.y + c2 * t2.y);
+  C m2 = cmk<C>(a0.x + c2 * t1.x + c1 * t2.x, a0.y + c2 * t1.y + c1 * t2.y);
+  C n1 = cmk<C>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+  C n2 = cmk<C>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+  v[0] = cadd(a0, cadd(t1, t2));
+  // y = m -/+ i n
+  v[1] = cmk<C>(m1.x + n1.y, m1.y - n1.x);
+  v[4] = cmk<C>(m1.x - n1.y, m1.y + n1.x);
+  v[2] = cmk<C>(m2.x + n2.y, m2.y - n2.x);
+  v[3] = cmk<C>(m2.x - n2.y, m2.y + n2.x);
+}
+
+template <typename C> __device__ __forceinline__ void dft7p(C* v) {
+  using T = decltype(C::x);
+  // cos(2 pi j / 7), sin(2 pi j / 7), j = 0..6
+  const T cs[7] = {T(1.0), T(0.62348980185873353053), T(-0.22252093395631440429),
+                   T(-0.90096886790241912624), T(-0.90096886790241912624),
+                   T(-0.22252093395631440429), T(0.62348980185873353053)};
+  const T sn[7] = {T(0.0), T(0.78183148246802980871), T(0.97492791218182360702),
+                   T(0.43388373911755812048), T(-0.43388373911755812048),
+                   T(-0.97492791218182360702), T(-0.78183148246802980871)};
+  C t[3], u[3];
+#pragma unroll
+  for (int k = 1; k <= 3; ++k) {
+    t[k - 1] = cadd(v[k], v[7 - k]);
+    u[k - 1] = csub(v[k], v[7 - k]);
+  }
+  C a0 = v[0];
+  v[0] = cadd(a0, cadd(t[0], cadd(t[1], t[2])));
+#pragma unroll
+  for (int m = 1; m <= 3; ++m) {
+    C re = a0, im = cmk<C>(T(0), T(0));
+#pragma unroll
+    for (int k = 1; k <= 3; ++k) {
+      const T c = cs[(k * m) % 7], s = sn[(k * m) % 7];
+      re = cmk<C>(re.x + c * t[k - 1].x, re.y + c * t[k - 1].y);
+      im = cmk<C>(im.x + s * u[k - 1].x, im.y + s * u[k - 1].y);
+    }
+    v[m] = cmk<C>(re.x + im.y, re.y - im.x);
+    v[7 - m] = cmk<C>(re.x - im.y, re.y + im.x);
+  }
+}
+
+template <typename C> __device__ __forceinline__ void dft8p(C* v) {
+  using T = decltype(C::x);
+  const T r2 = T(0.70710678118654752440);
+  dft4v(v[0], v[2], v[4], v[6]);
+  dft4v(v[1], v[3], v[5], v[7]);
+  // odd half times W8^k1 (k1 = 1..3); its values sit at v[1 + 2 k1]
+  C o1 = cmk<C>((v[3].x + v[3].y) * r2, (v[3].y - v[3].x) * r2);   // * (1 - i)/sqrt2
+  C o2 = cmul_mi(v[5]);                                               // * -i
+  C o3 = cmk<C>((v[7].y - v[7].x) * r2, -(v[7].x + v[7].y) * r2);  // * (-1 - i)/sqrt2
+  C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1];
+  v[0] = cadd(e0, o0);
+  v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1);
+  v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2);
+  v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3);
+  v[7] = csub(e3, o3);
+}
+
+template <typename C> __device__ __forceinline__ void dft16p(C* v) {
+  using T = decltype(C::x);
+  const T r2 = T(0.70710678118654752440);
+  const T c8 = T(0.92387953251128675613), s8 = T(0.38268343236508977173);
+  // n = j + 4 m, k = k1 + 4 k2: DFT4 over m for each j
+#pragma unroll
+  for (int j = 0; j < 4; ++j) dft4v(v[j], v[j + 4], v[j + 8], v[j + 12]);
+  // v[j + 4 k1] = b_j[k1]; multiply by W16^(j k1)
+  v[5] = cmul(v[5], cmk<C>(c8, -s8));                                    // W^1
+  v[9] = cmk<C>((v[9].x + v[9].y) * r2, (v[9].y - v[9].x) * r2);        // W^2
+  v[13] = cmul(v[13], cmk<C>(s8, -c8));                                  // W^3
+  v[6] = cmk<C>((v[6].x + v[6].y) * r2, (v[6].y - v[6].x) * r2);        // W^2
+  v[10] = cmul_mi(v[10]);                                                // W^4
+  v[14] = cmk<C>((v[14].y - v[14].x) * r2, -(v[14].x + v[14].y) * r2);  // W^6
+  v[7] = cmul(v[7], cmk<C>(s8, -c8));                                    // W^3
+  v[11] = cmk<C>((v[11].y - v[11].x) * r2, -(v[11].x + v[11].y) * r2);  // W^6
+  v[15] = cmul(v[15], cmk<C>(-c8, s8));                                  // W^9
+  // DFT4 over j for each k1; y[k1 + 4 k2] lands at v[4 k1 + k2]
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft4v(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+  C w[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) w[i] = v[i];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = w[4 * k1 + k2];
+}
+
+template <int R, typename C> __device__ __forceinline__ void dftp(C* v) {
+  if constexpr (R == 2) dft2p(v);
+  else if constexpr (R == 3) dft3p(v);
+  else if constexpr (R == 4) dft4p(v);
+  else if constexpr (R == 5) dft5p(v);
+  else if constexpr (R == 7) dft7p(v);
+  else if constexpr (R == 8) dft8p(v);
+  else if constexpr (R == 16) dft16p(v);
+}
+
+// ---------------------------------------------------------------------------
+// Per-thread view of one line: shared-memory slots and global addressing.
+// ---------------------------------------------------------------------------
+template <typename T, int KIND, bool CONTIG>
+struct LineCtx {
+  using C = Cx<T>;
+  const C* tw;
+  const void* src;
+  void* dst;
+  long long sb0, sb1, db0, db1, ssn, dsn;
+  int N, L, tpl, t, line;
+  bool valid, has1, inverse;
+
+  __device__ __forceinline__ void init(const PassArgs& a) {
+    tw = reinterpret_cast<const C*>(a.tw);
+    src = a.src;
+    dst = a.dst;
+    N = a.n;
+    L = a.L;
+    tpl = a.tpl;
+    inverse = a.inverse != 0;
+    ssn = a.s_src_n;
+    dsn = a.s_dst_n;
+    if (CONTIG) {
+      t = threadIdx.x;
+      line = threadIdx.y;
+    } else {
+      line = threadIdx.x;
+      t = threadIdx.y;
+    }
+    const long long cl = (long long)blockIdx.x * a.L + line;
+    const long long v = CONTIG ? 0 : (long long)blockIdx.y;
+    valid = cl < a.nlines;
+    if (KIND == K_C2C) {
+      has1 = false;
+      sb0 = CONTIG ? cl * a.s_src_l : cl + v * a.s_src_l;
+      db0 = CONTIG ? cl * a.s_dst_l : cl + v * a.s_dst_l;
+      sb1 = sb0;
+      db1 = db0;
+    } else {
+      const long long r0 = 2 * cl, r1 = 2 * cl + 1;
+      has1 = r1 < a.real_lines;
+      sb0 = CONTIG ? r0 * a.s_src_l : r0 + v * a.s_src_l;
+      sb1 = CONTIG ? r1 * a.s_src_l : r1 + v * a.s_src_l;
+      db0 = CONTIG ? r0 * a.s_dst_l : r0 + v * a.s_dst_l;
+      db1 = CONTIG ? r1 * a.s_dst_l : r1 + v * a.s_dst_l;
+    }
+  }
+
+  __device__ __forceinline__ int sidx(int n) const {
+    const int a = CONTIG ? line * N + n : n * L + line;
+    return a + (a >> 5);
+  }
+  __device__ __forceinline__ C twiddle(int e) const { return __ldg(tw + e); }
+
+  // Point n of the complex line this thread works on, as the forward
+  // transform must see it.
+  __device__ __forceinline__ C gload(int n) const {
+    if (!valid) return cmk<C>(T(0), T(0));
+    if (KIND == K_C2C) {
+      C x = reinterpret_cast<const C*>(src)[sb0 + n * ssn];
+      if (inverse) x.y = -x.y;
+      return x;
+    } else if (KIND == K_R2C) {
+      const T* s = reinterpret_cast<const T*>(src);
+      const T re = s[sb0 + n * ssn];
+      const T im = has1 ? s[sb1 + n * ssn] : T(0);
+      return cmk<C>(re, im);
+    } else {
+      // Hermitian extension of both half spectra (src/fft_generic.f90:318-330)
+      const C* s = reinterpret_cast<const C*>(src);
+      const bool low = 2 * n <= N;
+      const int m = low ? n : N - n;
+      C x1 = s[sb0 + m * ssn];
+      C x2 = has1 ? s[sb1 + m * ssn] : cmk<C>(T(0), T(0));
+      if (!low) {
+        x1.y = -x1.y;
+        x2.y = -x2.y;
+      }
+      if (n == 0 || 2 * n == N) {  // c2r ignores Im of the DC and Nyquist bins
+        x1.y = T(0);
+        x2.y = T(0);
+      }
+      // z = x1 + i x2, conjugated for the inverse-by-conjugation
+      return cmk<C>(x1.x - x2.y, -(x1.y + x2.x));
+    }
+  }
+
+  __device__ __forceinline__ void gstore(int n, C v) const {
+    if (!valid) return;
+    if (KIND == K_C2C) {
+      if (inverse) v.y = -v.y;
+      reinterpret_cast<C*>(dst)[db0 + n * dsn] = v;
+    } else if (KIND == K_C2R) {
+      T* d = reinterpret_cast<T*>(dst);
+      d[db0 + n * dsn] = v.x;
+      if (has1) d[db1 + n * dsn] = -v.y;
+    }
+  }
+
+  // r2c output: separate the two half spectra held in shared memory,
+  // X1 = (Z_k + conj Z_{n-k}) / 2, X2 = (Z_k - conj Z_{n-k}) / (2i).
+  __device__ __forceinline__ void store_r2c(const C* S) const {
+    if (!valid) return;
+    C* d = reinterpret_cast<C*>(dst);
+    const T h = T(0.5);
+#pragma unroll 1
+    for (int k = t; 2 * k <= N; k += tpl) {
+      const C zk = S[sidx(k)], zm = S[sidx(k == 0 ? 0 : N - k)];
+      d[db0 + k * dsn] = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
+      if (has1) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
+    }
+  }
+};
+
+}  // namespace dev
+}  // namespace gbfft

@@ -54,10 +54,25 @@ struct PassArgs {
   int nv;          // strided: extent of v (grid.y)
   int first_fused; // stage 0 reads global memory directly
   int last_fused;  // last stage writes global memory directly
+  int fast;        // 1: run the compile-time power-of-two kernel for n
   int radix[kMaxStages];
 };
 
-// Shared memory a pass needs for L lines of length n (padded layout).
+// Power-of-two lengths with a compile-time-planned kernel (fft_fast.cuh):
+// 16 points per thread, n / 16 threads per line.
+__host__ __device__ constexpr bool fast_length(int n) {
+  return n >= 16 && n <= 4096 && (n & (n - 1)) == 0;
+}
+constexpr int kFastMaxThreadsF32 = 512;
+constexpr int kFastMaxThreadsF64 = 256;
+
+cudaError_t launch_fast_f32_c2c(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+cudaError_t launch_fast_f32_real(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+cudaError_t launch_fast_f64_c2c(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+cudaError_t launch_fast_f64_real(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+
+// Shared memory the runtime-planned pass needs for L lines of length n
+// (two padded buffers); the power-of-two pass needs half of it.
 size_t pass_smem_bytes(int prec_bytes, int n, int L);
 
 // Enqueue one axis pass.  prec_bytes = 4 (float) or 8 (double).

@@ -45,6 +45,9 @@ WORKLOADS = {
     "r2c_c2r_360x270x210_f64_x": (360, 270, 210, 1, 8, "uniform"),
     "r2c_c2r_360x270x210_f32_x": (360, 270, 210, 1, 4, "uniform"),
     "r2c_c2r_256x256x256_f32_x": (256, 256, 256, 1, 4, "uniform"),
+    # profiling sizes: the x/y lines of the 1024x1024x512 grid at ~1/4 the memory
+    "r2c_c2r_1024x1024x128_f32_x": (1024, 1024, 128, 1, 4, "gauss_modes"),
+    "r2c_c2r_1024x64x512_f32_x": (1024, 64, 512, 1, 4, "gauss_modes"),
 }
 DEFAULT_WORKLOAD = "r2c_c2r_1024x1024x512_f32_x"
 
