@@ -5,7 +5,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/gbfft.h"
+#include "gbfft.h"
 #include "gbfft_internal.h"
 
 namespace {

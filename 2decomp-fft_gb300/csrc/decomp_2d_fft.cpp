@@ -10,7 +10,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/decomp_2d_fft.h"
+#include "decomp_2d_fft.h"
 #include "gbfft_internal.h"
 
 namespace {

@@ -15,12 +15,13 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
 
-#include "../../include/gbfft.h"
+#include "gbfft.h"
 #include "gbfft_internal.h"
 
 using namespace gbfft;
@@ -47,7 +48,9 @@ struct AxisPlan {
   int nst = 0;
   int radix[kMaxStages] = {0};
   int tpl = 1;        // threads per line
-  void* d_tw = nullptr;
+  int fast_e = 16;    // points per thread of the power-of-two kernel
+  void* d_tw = nullptr;   // exp(-2 pi i m / n), m = 0..n-1
+  void* d_twf = nullptr;  // stage-major table of the power-of-two kernel
 };
 
 // Split n into radix stages: 16s, then one 8/4/2 for the rest of the powers
@@ -119,23 +122,50 @@ std::vector<double> twiddles(int n) {
   return t;
 }
 
-int upload_twiddles(AxisPlan& p, int prec) {
-  std::vector<double> t = twiddles(p.n);
-  const size_t bytes = (size_t)p.n * 2 * (size_t)prec;
-  cudaError_t e = cudaMalloc(&p.d_tw, bytes);
+// Stage-major twiddles of the power-of-two kernel: stage s of radix R after
+// NS points holds W_{NS R}^{k r} at (NS - 1) + (r - 1) NS + k, for
+// r = 1..R-1, k = 0..NS-1 (n - 1 entries in all).
+std::vector<double> stage_twiddles(int n, int e) {
+  std::vector<double> t(2 * (size_t)n, 0.0);
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  int ns = 1;
+  for (int s = 0; s < fast_nst(n, e); ++s) {
+    const int R = fast_radix(n, e, s);
+    for (int r = 1; r < R; ++r)
+      for (int k = 0; k < ns; ++k) {
+        const long long m = ((long long)k * r) % ((long long)ns * R);
+        const long double a = two_pi * (long double)m / (long double)(ns * R);
+        const size_t i = (size_t)(ns - 1) + (size_t)(r - 1) * ns + k;
+        t[2 * i] = (double)cosl(a);
+        t[2 * i + 1] = (double)(-sinl(a));
+      }
+    ns *= R;
+  }
+  return t;
+}
+
+int upload_table(void** dst, const std::vector<double>& t, int prec) {
+  const size_t bytes = t.size() / 2 * 2 * (size_t)prec;
+  cudaError_t e = cudaMalloc(dst, bytes);
   if (e != cudaSuccess) {
-    p.d_tw = nullptr;
+    *dst = nullptr;
     return cuda_fail(e, "cudaMalloc(twiddles)");
   }
   if (prec == 8) {
-    e = cudaMemcpy(p.d_tw, t.data(), bytes, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(*dst, t.data(), bytes, cudaMemcpyHostToDevice);
   } else {
     std::vector<float> f(t.size());
     for (size_t i = 0; i < t.size(); ++i) f[i] = (float)t[i];
-    e = cudaMemcpy(p.d_tw, f.data(), bytes, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(*dst, f.data(), bytes, cudaMemcpyHostToDevice);
   }
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(twiddles)");
   return GBFFT_OK;
+}
+
+int upload_twiddles(AxisPlan& p, int prec) {
+  int rc = upload_table(&p.d_tw, twiddles(p.n), prec);
+  if (rc == GBFFT_OK && fast_length(p.n)) rc = upload_table(&p.d_twf, stage_twiddles(p.n, p.fast_e), prec);
+  return rc;
 }
 
 }  // namespace
@@ -162,6 +192,10 @@ struct gbfft_engine_s {
   int ph[3] = {0, 0, 0};
   int sp[3] = {0, 0, 0};
   AxisPlan ax[3];
+  int tile_L[GBFFT_PASS_KINDS] = {0};  // tuned lines per CTA, 0 = built-in
+  bool fuse = false;                   // fuse x/y passes per plane when possible
+  int* d_sync = nullptr;               // fused kernel's ticket/status/plane counters
+  long long sync_planes = 0;
   void* work = nullptr;
   size_t work_bytes = 0;
 };
@@ -182,18 +216,30 @@ void release(gbfft_engine_t e) {
   drop_profile(e);
   for (auto& a : e->ax) {
     if (a.d_tw) cudaFree(a.d_tw);
+    if (a.d_twf) cudaFree(a.d_twf);
     a.d_tw = nullptr;
+    a.d_twf = nullptr;
   }
   if (e->work) cudaFree(e->work);
   e->work = nullptr;
+  if (e->d_sync) cudaFree(e->d_sync);
+  e->d_sync = nullptr;
 }
 
 size_t cbytes(const gbfft_engine_s* e) { return 2 * (size_t)e->prec; }
 
 // Lines per CTA for a pass with the given plan.
-int lines_per_cta(const AxisPlan& p, int prec, bool contiguous, long long nlines, int* tpl_out) {
+int lines_per_cta(const AxisPlan& p, int prec, bool contiguous, long long nlines, int* tpl_out,
+                  int forced_L) {
   int tpl = p.tpl;
   int L;
+  if (forced_L > 0) {
+    L = forced_L;
+    if (!contiguous)
+      while (L * tpl > kMaxThreads && tpl > 32) tpl /= 2;
+    *tpl_out = tpl;
+    return L;
+  }
   if (contiguous) {
     L = 256 / tpl;
     if (L < 1) L = 1;
@@ -216,13 +262,19 @@ int lines_per_cta(const AxisPlan& p, int prec, bool contiguous, long long nlines
   return L < 1 ? 1 : L;
 }
 
-// Lines per CTA for the power-of-two kernel (n / 16 threads per line).
-int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines) {
-  const int tpl = n / 16;
-  const int maxt = prec == 4 ? kFastMaxThreadsF32 : kFastMaxThreadsF64;
+// Lines per CTA for the power-of-two kernel (n / fast_points(n) threads per
+// line).
+int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int forced_L) {
+  const int e = fast_points(n, contiguous);
+  const int tpl = n / e;
+  if (forced_L > 0) return forced_L;
+  const int maxt = fast_max_threads(e, prec);
   int L;
   if (contiguous) {
-    L = 256 / tpl;
+    // lines of at most 32 threads run warp-synchronous: 4 warps per CTA;
+    // longer lines: one line (pair) per CTA, so that many small CTAs per SM
+    // overlap their load, exchange and store phases
+    L = tpl > 32 ? 1 : 128 / tpl;
   } else {
     const int min_l = (int)(64 / (2 * prec));
     L = 512 / tpl;
@@ -230,8 +282,7 @@ int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines) {
     if (L < min_l) L = min_l;
   }
   while (L > 1 && L * tpl > maxt) L /= 2;
-  const size_t line_bytes = (size_t)n * 2 * prec;
-  while (L > 1 && (size_t)L * line_bytes > 96 * 1024) L /= 2;
+  while (L > 1 && (size_t)fast_smem_entries(n, L) * 2 * prec > 100 * 1024) L /= 2;
   if (L < 1) L = 1;
   if (L > 1 && nlines < L) {
     int l2 = 1;
@@ -242,14 +293,14 @@ int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines) {
 }
 
 // Fill the plan-dependent fields of a pass.
-void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind) {
+void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind, int forced_L) {
   if (fast_length(p.n)) {
     a.n = p.n;
     a.nst = 0;
-    a.tw = p.d_tw;
+    a.tw = p.d_twf;
     a.fast = 1;
-    a.tpl = p.n / 16;
-    a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines);
+    a.tpl = p.n / fast_points(p.n, contiguous);
+    a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L);
     a.first_fused = 1;
     a.last_fused = kind != K_R2C;
     (void)kind;
@@ -259,7 +310,7 @@ void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int ki
   a.nst = p.nst;
   for (int i = 0; i < kMaxStages; ++i) a.radix[i] = i < p.nst ? p.radix[i] : 0;
   a.tw = p.d_tw;
-  a.L = lines_per_cta(p, prec, contiguous, a.nlines, &a.tpl);
+  a.L = lines_per_cta(p, prec, contiguous, a.nlines, &a.tpl, forced_L);
   a.first_fused = 0;
   a.last_fused = 0;
   (void)kind;
@@ -271,6 +322,10 @@ struct Pass {
   bool contiguous;
   int prof_kind;   // GBFFT_PASS_*
   double bytes;    // algorithmic bytes: one read + one write of the array
+  bool fused = false;  // x and y passes of each z-plane in one kernel
+  FusedArgs f;
+  int fused_kindx = 0;
+  bool fused_xfirst = true;
 };
 
 // c2c along `axis` of a complex (n1, n2, n3) array.
@@ -302,7 +357,7 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
     a.nlines = n1;
     a.nv = n2;
   }
-  fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C);
+  fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C, e->tile_L[GBFFT_PASS_C2C_X + axis]);
   P.prof_kind = GBFFT_PASS_C2C_X + axis;
   P.bytes = 2.0 * (double)n1 * n2 * n3 * (double)cbytes(e);
   return P;
@@ -346,12 +401,66 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst) {
     a.s_dst_l = real_s_l;
     a.inverse = 1;
   }
+  // strided pairs are neighbouring x positions: 8-byte aligned when nx is
+  // even (every line then starts at an even real index)
+  const void* real_ptr = kind == K_R2C ? src : dst;
+  a.pair_vec = (!P.contiguous && nx % 2 == 0 && ((uintptr_t)real_ptr % (2 * (size_t)e->prec)) == 0) ? 1 : 0;
   const int axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
-  fill_plan(a, e->ax[axis], e->prec, P.contiguous, kind);
+  fill_plan(a, e->ax[axis], e->prec, P.contiguous, kind,
+            e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R]);
   P.prof_kind = kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R;
   P.bytes = (double)nx * ny * nz * e->prec +
             (double)e->sp[0] * e->sp[1] * e->sp[2] * (double)cbytes(e);
   return P;
+}
+
+// Replace an adjacent x pass / y pass (either order, each feeding the next)
+// by one fused x/y kernel when one exists for the lengths.  `planes` is the
+// z extent of the array the two passes work on.
+void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
+  if (!e->d_sync || planes > e->sync_planes) return;
+  for (size_t i = 0; i + 1 < ps.size(); ++i) {
+    Pass& p0 = ps[i];
+    Pass& p1 = ps[i + 1];
+    const bool x0 = p0.contiguous && (p0.prof_kind == GBFFT_PASS_C2C_X || p0.prof_kind == GBFFT_PASS_R2C ||
+                                      p0.prof_kind == GBFFT_PASS_C2R);
+    const bool x1 = p1.contiguous && (p1.prof_kind == GBFFT_PASS_C2C_X || p1.prof_kind == GBFFT_PASS_R2C ||
+                                      p1.prof_kind == GBFFT_PASS_C2R);
+    const bool y0 = p0.prof_kind == GBFFT_PASS_C2C_Y, y1 = p1.prof_kind == GBFFT_PASS_C2C_Y;
+    if (!((x0 && y1) || (y0 && x1))) continue;
+    const bool xfirst = x0;
+    Pass& px = xfirst ? p0 : p1;
+    Pass& py = xfirst ? p1 : p0;
+    if (p1.a.src != p0.a.dst) continue;
+    if (!fast_length(px.a.n) || !fast_length(py.a.n)) continue;
+    if (!fused_supported(e->prec, px.kind, xfirst, px.a.n, py.a.n)) continue;
+    long long per_plane;
+    if (px.kind == K_C2C) {
+      per_plane = px.a.nlines / planes;  // x lines of a c2c pass: n2 per plane
+    } else {
+      if (e->ny % 2) continue;  // line pairs must not straddle planes
+      per_plane = e->ny / 2;
+    }
+    if (per_plane * planes != px.a.nlines) continue;
+    Pass F = px;
+    F.fused = true;
+    F.fused_kindx = px.kind;
+    F.fused_xfirst = xfirst;
+    F.f.ax = px.a;
+    F.f.ax.nlines = (int)per_plane;
+    F.f.ax.tpl = px.a.n / fast_points(px.a.n, true);
+    F.f.ax.L = kFusedThreads / F.f.ax.tpl;
+    F.f.ay = py.a;
+    F.f.ay.tpl = py.a.n / fast_points(py.a.n, false);
+    F.f.ay.L = kFusedThreads / F.f.ay.tpl;
+    F.f.nplanes = planes;
+    F.f.sync = e->d_sync;
+    F.prof_kind = GBFFT_PASS_XY;
+    F.bytes = px.bytes + py.bytes;
+    ps[i] = F;
+    ps.erase(ps.begin() + i + 1);
+    return;
+  }
 }
 
 int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st) {
@@ -364,7 +473,8 @@ int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st) 
         return fail(GBFFT_ERR_CUDA, "cudaEventCreate");
       cudaEventRecord(rec.start, st);
     }
-    cudaError_t err = launch_axis_pass(e->prec, p.kind, p.contiguous, p.a, st);
+    cudaError_t err = p.fused ? launch_fused(e->prec, p.fused_kindx, p.fused_xfirst, p.f, st)
+                              : launch_axis_pass(e->prec, p.kind, p.contiguous, p.a, st);
     if (e->profiling) {
       cudaEventRecord(rec.stop, st);
       e->prof.push_back(rec);
@@ -373,6 +483,10 @@ int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st) 
   }
   return GBFFT_OK;
 }
+
+// Arrays must be aligned to their element: prec bytes for real arrays,
+// 2 * prec for complex ones (the kernels move whole elements).
+bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
 
 bool overlap(const void* a, size_t na, const void* b, size_t nb) {
   const char* pa = (const char*)a;
@@ -479,6 +593,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
       return fail(GBFFT_ERR_UNSUPPORTED, "axis length " + std::to_string(lens[d]) +
                                              " does not fit one shared-memory tile at this precision");
     }
+    e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
     int rc = upload_twiddles(e->ax[d], prec);
     if (rc != GBFFT_OK) {
       release(e);
@@ -497,6 +612,19 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
       g_err = std::string("cudaMalloc(work area): ") + cudaGetErrorString(err);
       return GBFFT_ERR_ALLOC;
     }
+  }
+  // counters of the fused x/y kernel: one per z-plane plus ticket and status
+  if (prec == GBFFT_PREC_SINGLE && fast_length(nx) && fast_length(ny)) {
+    e->sync_planes = nz;
+    cudaError_t err = cudaMalloc(&e->d_sync, (size_t)(nz + 2) * sizeof(int));
+    if (err != cudaSuccess) {
+      e->d_sync = nullptr;
+      release(e);
+      delete e;
+      g_err = std::string("cudaMalloc(counters): ") + cudaGetErrorString(err);
+      return GBFFT_ERR_ALLOC;
+    }
+    cudaMemset(e->d_sync, 0, (size_t)(nz + 2) * sizeof(int));
   }
   *engine = e;
   return GBFFT_OK;
@@ -533,6 +661,8 @@ int gbfft_exec_r2c(gbfft_engine_t e, const void* d_in, void* d_out, void* stream
   const size_t cb = (size_t)e->sp[0] * e->sp[1] * e->sp[2] * cbytes(e);
   if (overlap(d_in, rb, d_out, cb))
     return fail(GBFFT_ERR_INVALID, "In-place r2c transform is not yet available");
+  if (!aligned(d_in, e->prec) || !aligned(d_out, cbytes(e)))
+    return fail(GBFFT_ERR_INVALID, "array not aligned to its element size");
   cudaStream_t st = (cudaStream_t)stream;
   std::vector<Pass> ps;
   const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
@@ -547,6 +677,7 @@ int gbfft_exec_r2c(gbfft_engine_t e, const void* d_in, void* d_out, void* stream
     if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
     if (!e->skip[0]) ps.push_back(c2c_pass(e, 0, s1, s2, s3, d_out, d_out, 0));
   }
+  if (e->fuse) fuse_xy(e, ps, s3);
   return run_passes(e, ps, st);
 }
 
@@ -557,6 +688,8 @@ int gbfft_exec_c2r(gbfft_engine_t e, void* d_in, void* d_out, void* stream) {
   const size_t cb = (size_t)e->sp[0] * e->sp[1] * e->sp[2] * cbytes(e);
   if (overlap(d_in, cb, d_out, rb))
     return fail(GBFFT_ERR_INVALID, "In-place c2r transform is not yet available");
+  if (!aligned(d_in, cbytes(e)) || !aligned(d_out, e->prec))
+    return fail(GBFFT_ERR_INVALID, "array not aligned to its element size");
   cudaStream_t st = (cudaStream_t)stream;
   void* W = e->inplace ? d_in : e->work;
   if (!W) return fail(GBFFT_ERR_STATE, "engine has no work area");
@@ -576,6 +709,7 @@ int gbfft_exec_c2r(gbfft_engine_t e, void* d_in, void* d_out, void* stream) {
   if (e->format == GBFFT_PHYSICAL_IN_X && e->skip[0]) warn_skip(3);
   if (e->format == GBFFT_PHYSICAL_IN_Z && e->skip[2]) warn_skip(4);
   ps.push_back(real_pass(e, K_C2R, cur, d_out));
+  if (e->fuse) fuse_xy(e, ps, s3);
   return run_passes(e, ps, st);
 }
 
@@ -589,6 +723,8 @@ int gbfft_exec_c2c(gbfft_engine_t e, void* d_in, void* d_out, int isign, void* s
   const size_t bytes = (size_t)n1 * n2 * n3 * cbytes(e);
   if (d_in != d_out && overlap(d_in, bytes, d_out, bytes))
     return fail(GBFFT_ERR_INVALID, "input and output partially overlap");
+  if (!aligned(d_in, cbytes(e)) || !aligned(d_out, cbytes(e)))
+    return fail(GBFFT_ERR_INVALID, "array not aligned to its element size");
   const bool x_first = (e->format == GBFFT_PHYSICAL_IN_X && isign == GBFFT_FORWARD) ||
                        (e->format == GBFFT_PHYSICAL_IN_Z && isign == GBFFT_BACKWARD);
   const int order_f[3] = {0, 1, 2}, order_b[3] = {2, 1, 0};
@@ -607,6 +743,7 @@ int gbfft_exec_c2c(gbfft_engine_t e, void* d_in, void* d_out, int isign, void* s
     if (err != cudaSuccess) return cuda_fail(err, "copy launch");
     return GBFFT_OK;
   }
+  if (e->fuse) fuse_xy(e, ps, n3);
   return run_passes(e, ps, st);
 }
 
@@ -635,6 +772,58 @@ int gbfft_engine_set_profiling(gbfft_engine_t e, int enable) {
     e->prof_bytes[k] = 0;
   }
   e->profiling = enable != 0;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (kind < 0 || kind >= GBFFT_PASS_KINDS) return fail(GBFFT_ERR_INVALID, "bad pass kind");
+  if (lines < 0 || lines > 64) return fail(GBFFT_ERR_INVALID, "lines per CTA out of range");
+  if (lines == 0) {
+    e->tile_L[kind] = 0;
+    return GBFFT_OK;
+  }
+  int axis;
+  if (kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R)
+    axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
+  else
+    axis = kind - GBFFT_PASS_C2C_X;
+  const AxisPlan& p = e->ax[axis];
+  const bool fast = fast_length(p.n);
+  const bool contig_pass = (kind == GBFFT_PASS_C2C_X) ||
+                           ((kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R) &&
+                            e->format == GBFFT_PHYSICAL_IN_X);
+  const int fe = fast_points(p.n, contig_pass);
+  int tpl = fast ? p.n / fe : p.tpl;
+  const int maxt = fast ? fast_max_threads(fe, e->prec) : kMaxThreads;
+  if (!fast) {
+    const bool contiguous = (kind == GBFFT_PASS_C2C_X) ||
+                            ((kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R) &&
+                             e->format == GBFFT_PHYSICAL_IN_X);
+    if (!contiguous)
+      while (lines * tpl > kMaxThreads && tpl > 32) tpl /= 2;
+  }
+  if (lines * tpl > maxt) return fail(GBFFT_ERR_INVALID, "tile exceeds the kernel's thread limit");
+  const size_t smem = fast ? (size_t)fast_smem_entries(p.n, lines) * 2 * (size_t)e->prec
+                            : pass_smem_bytes(e->prec, p.n, lines);
+  if (smem > 200 * 1024) return fail(GBFFT_ERR_INVALID, "tile exceeds the shared-memory limit");
+  e->tile_L[kind] = lines;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_status(gbfft_engine_t e) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (!e->d_sync) return GBFFT_OK;
+  int flag = 0;
+  cudaError_t err = cudaMemcpy(&flag, e->d_sync + 1, sizeof(int), cudaMemcpyDeviceToHost);
+  if (err != cudaSuccess) return cuda_fail(err, "cudaMemcpy(status)");
+  if (flag) return fail(GBFFT_ERR_TIMEOUT, "a fused pass gave up waiting for its plane");
+  return GBFFT_OK;
+}
+
+int gbfft_engine_set_fusion(gbfft_engine_t e, int enable) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  e->fuse = enable != 0;
   return GBFFT_OK;
 }
 

@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(kMaxThreads)
   c.init(a);
   const size_t e = (size_t)a.n * a.L;
   C* buf0 = reinterpret_cast<C*>(smem_raw);
-  C* buf1 = buf0 + (e + (e >> 5) + 1);
+  C* buf1 = buf0 + (e + (e >> 4) + 1);
 
 #pragma unroll 1
   for (int n = c.t; n < c.N; n += c.tpl) buf0[c.sidx(n)] = c.gload(n);
@@ -193,7 +193,7 @@ int sm_count() {
 
 size_t pass_smem_bytes(int prec_bytes, int n, int L) {
   const size_t e = (size_t)n * (size_t)L;
-  return 2 * (e + (e >> 5) + 1) * (size_t)(2 * prec_bytes);
+  return 2 * (e + (e >> 4) + 1) * (size_t)(2 * prec_bytes);
 }
 
 cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a,

@@ -155,6 +155,33 @@ template <typename C> __device__ __forceinline__ void dft16p(C* v) {
     for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = w[4 * k1 + k2];
 }
 
+// Radix 32 as two radix-16 halves (even / odd points) joined by W32^k.
+template <typename C> __device__ __forceinline__ void dft32p(C* v) {
+  using T = decltype(C::x);
+  // cos(pi k / 16), k = 0..8
+  const T c[9] = {T(1.0), T(0.98078528040323044913), T(0.92387953251128675613),
+                  T(0.83146961230254523708), T(0.70710678118654752440), T(0.55557023301960222474),
+                  T(0.38268343236508977173), T(0.19509032201612826785), T(0.0)};
+  C e[16], o[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    e[i] = v[2 * i];
+    o[i] = v[2 * i + 1];
+  }
+  dft16p(e);
+  dft16p(o);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    // W32^k = cos(pi k/16) - i sin(pi k/16); sin(pi k/16) = cos(pi (8-k)/16)
+    C w;
+    if (k <= 8) w = cmk<C>(c[k], -c[8 - k]);
+    else w = cmk<C>(-c[16 - k], -c[k - 8]);
+    C t = (k == 0) ? o[k] : (k == 8 ? cmul_mi(o[k]) : cmul(o[k], w));
+    v[k] = cadd(e[k], t);
+    v[k + 16] = csub(e[k], t);
+  }
+}
+
 template <int R, typename C> __device__ __forceinline__ void dftp(C* v) {
   if constexpr (R == 2) dft2p(v);
   else if constexpr (R == 3) dft3p(v);
@@ -163,22 +190,40 @@ template <int R, typename C> __device__ __forceinline__ void dftp(C* v) {
   else if constexpr (R == 7) dft7p(v);
   else if constexpr (R == 8) dft8p(v);
   else if constexpr (R == 16) dft16p(v);
+  else if constexpr (R == 32) dft32p(v);
 }
 
 // ---------------------------------------------------------------------------
 // Per-thread view of one line: shared-memory slots and global addressing.
 // ---------------------------------------------------------------------------
-template <typename T, int KIND, bool CONTIG>
+// CG: read sources through L2 only (ld.global.cg), for data other CTAs of
+// the same kernel wrote moments earlier.
+template <typename T, int KIND, bool CONTIG, bool CG = false>
 struct LineCtx {
   using C = Cx<T>;
+  using real_t = T;
+  static constexpr int kind = KIND;
+  static constexpr bool contiguous = CONTIG;
   const C* tw;
   const void* src;
   void* dst;
   long long sb0, sb1, db0, db1, ssn, dsn;
   int N, L, tpl, t, line;
-  bool valid, has1, inverse;
+  bool valid, has1, inverse, pvec;
 
   __device__ __forceinline__ void init(const PassArgs& a) {
+    if (CONTIG)
+      init_at(a, threadIdx.x, threadIdx.y, (long long)blockIdx.x * a.L + threadIdx.y, 0, a.nlines);
+    else
+      init_at(a, threadIdx.y, threadIdx.x, (long long)blockIdx.x * a.L + threadIdx.x,
+              (long long)blockIdx.y, a.nlines);
+  }
+
+  // Thread `t_` of line `line_` of a tile; cl is the complex line (its u
+  // index on strided axes), v the strided axes' second index, and lines at
+  // or past `limit` are padding.
+  __device__ __forceinline__ void init_at(const PassArgs& a, int t_, int line_, long long cl, long long v,
+                                          long long limit) {
     tw = reinterpret_cast<const C*>(a.tw);
     src = a.src;
     dst = a.dst;
@@ -188,16 +233,10 @@ struct LineCtx {
     inverse = a.inverse != 0;
     ssn = a.s_src_n;
     dsn = a.s_dst_n;
-    if (CONTIG) {
-      t = threadIdx.x;
-      line = threadIdx.y;
-    } else {
-      line = threadIdx.x;
-      t = threadIdx.y;
-    }
-    const long long cl = (long long)blockIdx.x * a.L + line;
-    const long long v = CONTIG ? 0 : (long long)blockIdx.y;
-    valid = cl < a.nlines;
+    pvec = !CONTIG && a.pair_vec;
+    t = t_;
+    line = line_;
+    valid = cl < limit;
     if (KIND == K_C2C) {
       has1 = false;
       sb0 = CONTIG ? cl * a.s_src_l : cl + v * a.s_src_l;
@@ -214,32 +253,41 @@ struct LineCtx {
     }
   }
 
+  // One pad slot every 16 entries: 8-byte values are served per half-warp
+  // and 16-byte values per quarter-warp, and this spacing keeps radix-16
+  // strided writes on distinct banks within each of them.
   __device__ __forceinline__ int sidx(int n) const {
     const int a = CONTIG ? line * N + n : n * L + line;
-    return a + (a >> 5);
+    return a + (a >> 4);
   }
   __device__ __forceinline__ C twiddle(int e) const { return __ldg(tw + e); }
 
   // Point n of the complex line this thread works on, as the forward
   // transform must see it.
+  template <typename V> __device__ __forceinline__ static V ld(const V* p) {
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+  }
+
   __device__ __forceinline__ C gload(int n) const {
     if (!valid) return cmk<C>(T(0), T(0));
     if (KIND == K_C2C) {
-      C x = reinterpret_cast<const C*>(src)[sb0 + n * ssn];
+      C x = ld(reinterpret_cast<const C*>(src) + sb0 + n * ssn);
       if (inverse) x.y = -x.y;
       return x;
     } else if (KIND == K_R2C) {
       const T* s = reinterpret_cast<const T*>(src);
-      const T re = s[sb0 + n * ssn];
-      const T im = has1 ? s[sb1 + n * ssn] : T(0);
+      if (!CONTIG && pvec && has1) return ld(reinterpret_cast<const C*>(s + sb0 + n * ssn));
+      const T re = ld(s + sb0 + n * ssn);
+      const T im = has1 ? ld(s + sb1 + n * ssn) : T(0);
       return cmk<C>(re, im);
     } else {
       // Hermitian extension of both half spectra (src/fft_generic.f90:318-330)
       const C* s = reinterpret_cast<const C*>(src);
       const bool low = 2 * n <= N;
       const int m = low ? n : N - n;
-      C x1 = s[sb0 + m * ssn];
-      C x2 = has1 ? s[sb1 + m * ssn] : cmk<C>(T(0), T(0));
+      C x1 = ld(s + sb0 + m * ssn);
+      C x2 = has1 ? ld(s + sb1 + m * ssn) : cmk<C>(T(0), T(0));
       if (!low) {
         x1.y = -x1.y;
         x2.y = -x2.y;
@@ -260,9 +308,62 @@ struct LineCtx {
       reinterpret_cast<C*>(dst)[db0 + n * dsn] = v;
     } else if (KIND == K_C2R) {
       T* d = reinterpret_cast<T*>(dst);
+      if (!CONTIG && pvec && has1) {
+        *reinterpret_cast<C*>(d + db0 + n * dsn) = cmk<C>(v.x, -v.y);
+        return;
+      }
       d[db0 + n * dsn] = v.x;
       if (has1) d[db1 + n * dsn] = -v.y;
     }
+  }
+
+  // c2r input staging: the two half spectra of this line pair (n/2+1 points
+  // each) in shared memory, slot j of half h at sstage(h (n/2+1) + j).
+  __device__ __forceinline__ int sstage(int j) const {
+    const int a = CONTIG ? line * (N + 2) + j : j * L + line;
+    return a + (a >> 4);
+  }
+  // NN, TPL: the line length and threads per line, known at compile time so
+  // that every load is issued before the first shared-memory store.
+  template <int NN, int TPL>
+  __device__ __forceinline__ void stage_c2r(C* S) const {
+    constexpr int h = NN / 2 + 1;
+    constexpr int J = (h + TPL - 1) / TPL;
+    const C* s = reinterpret_cast<const C*>(src);
+    C a[J], b[J];
+#pragma unroll
+    for (int i = 0; i < J; ++i) {
+      const int j = t + i * TPL;
+      const bool in = valid && j < h;
+      a[i] = in ? ld(s + sb0 + j * ssn) : cmk<C>(T(0), T(0));
+      b[i] = (in && has1) ? ld(s + sb1 + j * ssn) : cmk<C>(T(0), T(0));
+    }
+#pragma unroll
+    for (int i = 0; i < J; ++i) {
+      const int j = t + i * TPL;
+      if (j < h) {
+        S[sstage(j)] = a[i];
+        S[sstage(h + j)] = b[i];
+      }
+    }
+  }
+  // Point n of the complex line z = x1 + i x2 built from the staged half
+  // spectra by the Hermitian extension (src/fft_generic.f90:318-330),
+  // conjugated for the inverse-by-conjugation.
+  __device__ __forceinline__ C sgather_c2r(const C* S, int n) const {
+    const int h = N / 2 + 1;
+    const bool low = 2 * n <= N;
+    const int m = low ? n : N - n;
+    C x1 = S[sstage(m)], x2 = S[sstage(h + m)];
+    if (!low) {
+      x1.y = -x1.y;
+      x2.y = -x2.y;
+    }
+    if (n == 0 || 2 * n == N) {  // c2r ignores Im of the DC and Nyquist bins
+      x1.y = T(0);
+      x2.y = T(0);
+    }
+    return cmk<C>(x1.x - x2.y, -(x1.y + x2.x));
   }
 
   // r2c output: separate the two half spectra held in shared memory,

@@ -2,15 +2,20 @@
 //
 // Same job and addressing as the runtime-planned kernel (fft_axis.cu), laid
 // out for throughput:
-//  * each thread owns E = 16 points of its line in registers (TPL = n/16
-//    threads per line); every stage is radix 16 except the last, which takes
-//    the remaining factor 2, 4 or 8;
+//  * each thread owns E points of its line in registers (TPL = n/E threads
+//    per line): 512 and 1024 run as two stages (32 x 16, 32 x 32) with
+//    E = 32; the other lengths run radix 16 stages and a last stage of the
+//    remaining factor 2, 4 or 8 with E = 16;
 //  * stage 0 loads its 16 points straight from global memory -- all 16 loads
 //    in flight per thread, consecutive threads on consecutive points (or, on
 //    strided axes, consecutive x positions) -- and the last stage stores
 //    straight to global memory in the same coalesced order;
 //  * between stages the line is exchanged in place through one padded
-//    shared-memory buffer (one pad slot every 32 points);
+//    shared-memory buffer (one pad slot every 16 points);
+//  * twiddles come from a stage-major table (a.tw): stage s of radix R that
+//    follows NS = R_0...R_{s-1} points finds W_{NS R}^{k r} at
+//    (NS - 1) + (r - 1) NS + k, so the lanes of a warp read consecutive
+//    entries; the stage offsets telescope and the table has n - 1 entries;
 //  * every index, stride and twiddle exponent is a compile-time function of
 //    the thread index, so no integer division is left in the loop body.
 #pragma once
@@ -22,17 +27,12 @@ namespace fast {
 
 using namespace dev;
 
-constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
-
-template <int N>
+template <int N, int E_>
 struct P2Plan {
-  static constexpr int LOG = ilog2(N);
-  static constexpr int NFULL = LOG / 4;
-  static constexpr int REM = LOG % 4;
-  static constexpr int NST = NFULL + (REM ? 1 : 0);
-  static constexpr int E = 16;
+  static constexpr int E = E_;
+  static constexpr int NST = fast_nst(N, E);
   static constexpr int TPL = N / E;
-  __host__ __device__ static constexpr int radix(int s) { return s < NFULL ? 16 : (1 << REM); }
+  __host__ __device__ static constexpr int radix(int s) { return fast_radix(N, E, s); }
   __host__ __device__ static constexpr int ns(int s) {
     int v = 1;
     for (int i = 0; i < s; ++i) v *= radix(i);
@@ -40,16 +40,33 @@ struct P2Plan {
   }
 };
 
-template <typename T, int KIND, bool CONTIG, int N, int S>
-__device__ __forceinline__ void run_stages(const LineCtx<T, KIND, CONTIG>& c, Cx<T>* Sm,
-                                           Cx<T> (&v)[16]) {
-  using P = P2Plan<N>;
+// Barrier between stages: a line whose threads all sit in one warp
+// (contiguous lines, at most 32 threads per line) only needs the warp.
+template <bool WARP_LOCAL> __device__ __forceinline__ void stage_barrier() {
+  if constexpr (WARP_LOCAL) __syncwarp();
+  else __syncthreads();
+}
+
+template <int N, int E, int S, class Ctx, class C>
+__device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
+  using P = P2Plan<N, E>;
+  constexpr int KIND = Ctx::kind;
+  constexpr bool WL = Ctx::contiguous && P::TPL <= 32;
   if constexpr (S < P::NST) {
     constexpr int R = P::radix(S), NS = P::ns(S), MB = P::E / R, NB = N / R, TPL = P::TPL;
     constexpr bool FIRST = (S == 0), LAST = (S == P::NST - 1);
-    constexpr int TSTRIDE = N / (NS * R);
     const int t = c.t;
-    if constexpr (FIRST) {
+    if constexpr (FIRST && KIND == K_C2R) {
+      // half spectra staged in shared memory (each value read from global
+      // memory once, coalesced), then the Hermitian gather
+      c.template stage_c2r<N, TPL>(Sm);
+      __syncthreads();
+#pragma unroll
+      for (int m = 0; m < MB; ++m)
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[m * R + r] = c.sgather_c2r(Sm, t + m * TPL + r * NB);
+      __syncthreads();
+    } else if constexpr (FIRST) {
 #pragma unroll
       for (int m = 0; m < MB; ++m)
 #pragma unroll
@@ -66,7 +83,7 @@ __device__ __forceinline__ void run_stages(const LineCtx<T, KIND, CONTIG>& c, Cx
       const int k = b & (NS - 1);
       if constexpr (NS > 1) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[m * R + r] = cmul(v[m * R + r], c.twiddle(k * r * TSTRIDE));
+        for (int r = 1; r < R; ++r) v[m * R + r] = cmul(v[m * R + r], c.twiddle((NS - 1) + (r - 1) * NS + k));
       }
       dftp<R>(&v[m * R]);
     }
@@ -80,7 +97,7 @@ __device__ __forceinline__ void run_stages(const LineCtx<T, KIND, CONTIG>& c, Cx
         for (int r = 0; r < R; ++r) c.gstore(base + r * NS, v[m * R + r]);
       }
     } else {
-      if constexpr (!FIRST) __syncthreads();
+      if constexpr (!FIRST) stage_barrier<WL>();
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         const int b = t + m * TPL;
@@ -89,34 +106,41 @@ __device__ __forceinline__ void run_stages(const LineCtx<T, KIND, CONTIG>& c, Cx
 #pragma unroll
         for (int r = 0; r < R; ++r) Sm[c.sidx(base + r * NS)] = v[m * R + r];
       }
-      __syncthreads();
+      // the r2c split after the last stage reads other lines' points
+      if constexpr (LAST) __syncthreads();
+      else stage_barrier<WL>();
     }
-    run_stages<T, KIND, CONTIG, N, S + 1>(c, Sm, v);
+    run_stages<N, E, S + 1>(c, Sm, v);
   }
 }
 
+// 16 points a thread, FP32: at most 512 threads and two CTAs per SM, i.e.
+// at most 64 registers a thread, so a 512-thread strided tile still runs two
+// CTAs per SM.  32 points a thread: at most 256 threads and two CTAs per SM
+// (128 registers).
 template <typename T, int KIND, bool CONTIG, int N>
-__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256)
+__global__ void __launch_bounds__(fast_max_threads(fast_points(N, CONTIG), sizeof(T)), sizeof(T) == 4 ? 2 : 1)
     fast_pass_kernel(const __grid_constant__ PassArgs a) {
+  constexpr int E = fast_points(N, CONTIG);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* Sm = reinterpret_cast<Cx<T>*>(smem_raw);
   LineCtx<T, KIND, CONTIG> c;
   c.init(a);
-  Cx<T> v[16];
-  run_stages<T, KIND, CONTIG, N, 0>(c, Sm, v);
+  Cx<T> v[E];
+  run_stages<N, E, 0>(c, Sm, v);
   if constexpr (KIND == K_R2C) c.store_r2c(Sm);
 }
 
 template <typename T, int KIND, bool CONTIG, int N>
 cudaError_t launch_n(const PassArgs& a, cudaStream_t stream) {
-  const size_t e = (size_t)N * a.L;
-  const size_t smem = (e + (e >> 5) + 1) * sizeof(Cx<T>);
+  const size_t smem = (size_t)fast_smem_entries(N, a.L) * sizeof(Cx<T>);
   auto kern = fast_pass_kernel<T, KIND, CONTIG, N>;
   if (smem > 48 * 1024) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
   }
-  const dim3 block = CONTIG ? dim3(P2Plan<N>::TPL, a.L) : dim3(a.L, P2Plan<N>::TPL);
+  constexpr int TPL = N / fast_points(N, CONTIG);
+  const dim3 block = CONTIG ? dim3(TPL, a.L) : dim3(a.L, TPL);
   const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
   kern<<<grid, block, smem, stream>>>(a);
   add_launches(1);

@@ -55,6 +55,8 @@ struct PassArgs {
   int first_fused; // stage 0 reads global memory directly
   int last_fused;  // last stage writes global memory directly
   int fast;        // 1: run the compile-time power-of-two kernel for n
+  int pair_vec;    // r2c/c2r on strided lines: the two real lines of a pair
+                   // are adjacent and 8-byte aligned (read/write as one pair)
   int radix[kMaxStages];
 };
 
@@ -63,13 +65,54 @@ struct PassArgs {
 __host__ __device__ constexpr bool fast_length(int n) {
   return n >= 16 && n <= 4096 && (n & (n - 1)) == 0;
 }
+// Radix plan of the power-of-two kernel, for E points per thread.  E = 32
+// (strided y/z lines of length 512 or 1024): two stages, 32 x (n/32), one
+// exchange.  E = 16 (everything else): radix 16 stages, then one stage of
+// the remaining factor 2, 4 or 8.
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+__host__ __device__ constexpr int fast_points(int n, bool contiguous) {
+  return (!contiguous && (n == 512 || n == 1024)) ? 32 : 16;
+}
+__host__ __device__ constexpr int fast_nst(int n, int e) {
+  return e == 32 ? 2 : ilog2c(n) / 4 + (ilog2c(n) % 4 ? 1 : 0);
+}
+__host__ __device__ constexpr int fast_radix(int n, int e, int s) {
+  return e == 32 ? (s == 0 ? 32 : n / 32) : (s < ilog2c(n) / 4 ? 16 : (1 << (ilog2c(n) % 4)));
+}
 constexpr int kFastMaxThreadsF32 = 512;
 constexpr int kFastMaxThreadsF64 = 256;
+// Thread limit of the power-of-two kernel for E points a thread.
+__host__ __device__ constexpr int fast_max_threads(int e, int prec_bytes) {
+  return e == 32 ? 256 : (prec_bytes == 4 ? kFastMaxThreadsF32 : kFastMaxThreadsF64);
+}
+// Shared-memory entries of one power-of-two tile of L lines: the exchange
+// buffer, or for c2r the staged half spectra (n/2+1 per real line).
+__host__ __device__ constexpr long long fast_smem_entries(int n, int L) {
+  return (long long)(n + 2) * L + (((long long)(n + 2) * L) >> 4) + 1;
+}
 
 cudaError_t launch_fast_f32_c2c(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 cudaError_t launch_fast_f32_real(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 cudaError_t launch_fast_f64_c2c(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 cudaError_t launch_fast_f64_real(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+
+// The x and y passes of one z-plane run by one fused kernel
+// (fft_fused.cuh): ax holds the x pass with ax.nlines = complex x lines per
+// plane, ay the y pass (ay.nlines = columns, ay.nv = planes).
+struct FusedArgs {
+  PassArgs ax;
+  PassArgs ay;
+  long long nplanes;
+  int* sync;  // nplanes + 2 ints: ticket, error flag, per-plane counters
+};
+
+// True when a fused x/y kernel exists for these lengths (x first or y
+// first, x kind K_C2C / K_R2C / K_C2R).
+bool fused_supported(int prec_bytes, int kindx, bool x_first, int nx, int ny);
+// Threads per CTA of the fused kernel (one tile of L = 512 / (n / 16) lines).
+constexpr int kFusedThreads = 512;
+// Enqueue a fused x/y pass (zeroes f.sync first).
+cudaError_t launch_fused(int prec_bytes, int kindx, bool x_first, const FusedArgs& f, cudaStream_t stream);
 
 // Shared memory the runtime-planned pass needs for L lines of length n
 // (two padded buffers); the power-of-two pass needs half of it.

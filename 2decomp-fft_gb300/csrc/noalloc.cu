@@ -29,7 +29,7 @@
 #include <cmath>
 #include <cstdio>
 
-#include "../../include/gbfft.h"
+#include "gbfft.h"
 #include "gbfft_internal.h"
 
 namespace {

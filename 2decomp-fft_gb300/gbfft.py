@@ -33,7 +33,7 @@ PREC_DOUBLE = 8
 FORM_PLAIN = 0
 FORM_SPLIT = 1
 X_TO_Y, Y_TO_Z, Z_TO_Y, Y_TO_X = 0, 1, 2, 3
-PASS_NAMES = ["r2c", "c2r", "c2c_x", "c2c_y", "c2c_z"]
+PASS_NAMES = ["r2c", "c2r", "c2c_x", "c2c_y", "c2c_z", "xy_fused"]
 D2D_FFT_BACKEND = 5
 
 # Every symbol the two public headers declare, with (restype, argtypes).
@@ -59,6 +59,9 @@ SIGNATURES = {
     "gbfft_batch_graph_launch": (_i, [_vp, _vp]),
     "gbfft_batch_destroy": (_i, [_vp]),
     "gbfft_engine_set_profiling": (_i, [_vp, _i]),
+    "gbfft_engine_set_tile": (_i, [_vp, _i, _i]),
+    "gbfft_engine_set_fusion": (_i, [_vp, _i]),
+    "gbfft_engine_status": (_i, [_vp]),
     "gbfft_engine_profile_read": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "gbfft_exec_c2r_noalloc": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp]),
@@ -203,6 +206,20 @@ class Engine:
     def c2c(self, x, out, isign, stream=None):
         check(lib().gbfft_exec_c2c(self.h, _ptr(x), _ptr(out), int(isign), _stream(stream)))
         return out
+
+    def set_tile(self, kind, lines):
+        """Lines per CTA of pass kind (index into PASS_NAMES); 0 = built-in."""
+        if isinstance(kind, str):
+            kind = PASS_NAMES.index(kind)
+        check(lib().gbfft_engine_set_tile(self.h, int(kind), int(lines)))
+
+    def set_fusion(self, enable):
+        """Fuse the x and y passes of each z-plane into one kernel (default on)."""
+        check(lib().gbfft_engine_set_fusion(self.h, int(bool(enable))))
+
+    def status(self):
+        """Raise GbfftError if the last fused pass gave up on a bounded wait."""
+        check(lib().gbfft_engine_status(self.h))
 
     def set_profiling(self, enable):
         check(lib().gbfft_engine_set_profiling(self.h, int(bool(enable))))

@@ -11,7 +11,8 @@
  *
  * Array layout: a 3D array (n1, n2, n3) is stored with the first index
  * fastest (Fortran order), as every 2DECOMP pencil is.  Complex values are
- * interleaved (re, im).  At one rank the X-, Y- and Z-pencil of a field share
+ * interleaved (re, im).  Arrays must be aligned to their element size
+ * (sizeof(real) for real arrays, 2 * sizeof(real) for complex ones).  At one rank the X-, Y- and Z-pencil of a field share
  * the same shape and the same layout.
  */
 #ifndef GBFFT_H
@@ -148,8 +149,26 @@ int gbfft_batch_destroy(gbfft_batch_t batch);
 #define GBFFT_PASS_C2C_X 2
 #define GBFFT_PASS_C2C_Y 3
 #define GBFFT_PASS_C2C_Z 4
-#define GBFFT_PASS_KINDS 5
+#define GBFFT_PASS_XY 5   /* x and y passes fused per z-plane (one kernel) */
+#define GBFFT_PASS_KINDS 6
 int gbfft_engine_set_profiling(gbfft_engine_t engine, int enable);
+
+/* Tile shape of one pass kind (GBFFT_PASS_*): lines per CTA.  0 restores the
+ * built-in choice.  Used by the autotuner; rejected when the CTA would exceed
+ * the kernel's thread or shared-memory limit. */
+int gbfft_engine_set_tile(gbfft_engine_t engine, int kind, int lines_per_cta);
+
+/* Pass fusion: 1 (default) lets the engine run the x and y passes of each
+ * z-plane in one kernel where a fused kernel exists for the lengths; 0 runs
+ * one kernel per axis. */
+int gbfft_engine_set_fusion(gbfft_engine_t engine, int enable);
+
+/* Status of the engine's most recent fused x/y pass: waits for the device,
+ * returns GBFFT_ERR_TIMEOUT if one of its bounded inter-CTA waits gave up
+ * (the result of that transform is then invalid), GBFFT_OK otherwise.  The
+ * fused pass keeps per-engine counters, so one engine must not run two
+ * transforms at the same time on different streams. */
+int gbfft_engine_status(gbfft_engine_t engine);
 int gbfft_engine_profile_read(gbfft_engine_t engine, int kind, long long* launches,
                               double* ms, double* bytes);
 

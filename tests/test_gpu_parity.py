@@ -74,6 +74,37 @@ def test_c2c_against_oracle(gpu, prec, fmt, isign, shape):
     assert rel(got, ref) <= TOL[prec]
 
 
+# Plane shapes with a fused x/y kernel (FP32, square power-of-two planes),
+# fused and unfused, against the FP64 oracle.
+@pytest.mark.parametrize("fuse", [True, False])
+@pytest.mark.parametrize("fmt", [O.PHYSICAL_IN_X, O.PHYSICAL_IN_Z])
+@pytest.mark.parametrize("shape", [(256, 256, 6), (512, 512, 3), (1024, 1024, 2), (256, 256, 1)])
+def test_fused_planes_against_oracle(fuse, fmt, shape):
+    import gbfft
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx + nz + fmt)
+    x = rng.standard_normal((nz, ny, nx))
+    e = gbfft.Engine(fmt, nx, ny, nz, prec=gbfft.PREC_SINGLE)
+    e.set_fusion(fuse)
+    xd = torch.from_numpy(x.astype(np.float32)).cuda()
+    s = e.empty_spectral()
+    e.r2c(xd, s)
+    ref = O.fft3d_r2c(x, fmt)
+    assert rel(s.cpu().numpy(), ref) <= TOL["s"]
+    sp = ref + 0.1 * (rng.standard_normal(ref.shape) + 1j * rng.standard_normal(ref.shape))
+    y = e.empty_physical()
+    e.c2r(torch.from_numpy(sp.astype(np.complex64)).cuda(), y)
+    assert rel(y.cpu().numpy(), O.fft3d_c2r(sp.copy(), nx, ny, nz, fmt)) <= TOL["s"]
+    c = x + 1j * rng.standard_normal(x.shape)
+    cd = torch.from_numpy(c.astype(np.complex64)).cuda()
+    for isign in (O.FORWARD, O.BACKWARD):
+        o = torch.empty_like(cd)
+        e.c2c(cd, o, isign)
+        assert rel(o.cpu().numpy(), O.fft3d_c2c(c.copy(), fmt, isign)) <= TOL["s"]
+    e.status()  # no bounded wait of a fused pass gave up
+    e.close()
+
+
 SKIPS = [(True, False, True), (False, True, False), (True, True, True), (False, False, True),
          (True, False, False)]
 
@@ -278,3 +309,40 @@ def test_batch_and_graph_match_single_engines():
         n = e.nx * e.ny * e.nz
         assert torch.allclose(x / n, x0, atol=2e-5)
     batch.close()
+
+
+def test_misaligned_arrays_are_rejected():
+    import gbfft
+    e = gbfft.Engine(gbfft.PHYSICAL_IN_X, 8, 8, 8, prec=gbfft.PREC_SINGLE)
+    buf = torch.zeros(4096, dtype=torch.float32, device="cuda")
+    spec = torch.zeros(8 * 8 * 5 + 2, dtype=torch.complex64, device="cuda")
+    base = spec.data_ptr()
+    with pytest.raises(gbfft.GbfftError, match="aligned"):
+        gbfft.check(gbfft.lib().gbfft_exec_r2c(e.h, buf.data_ptr(), base + 4, None))
+    with pytest.raises(gbfft.GbfftError, match="aligned"):
+        gbfft.check(gbfft.lib().gbfft_exec_r2c(e.h, buf.data_ptr() + 2, base, None))
+    e.close()
+
+
+@pytest.mark.parametrize("fmt", [O.PHYSICAL_IN_X, O.PHYSICAL_IN_Z])
+def test_real_array_at_odd_element_offset(fmt):
+    # a real array starting at an odd float: the strided pair loads/stores
+    # must fall back to single elements
+    import gbfft
+    nx, ny, nz = 16, 8, 32
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal((nz, ny, nx)).astype(np.float32)
+    e = gbfft.Engine(fmt, nx, ny, nz, prec=gbfft.PREC_SINGLE)
+    raw = torch.zeros(nx * ny * nz + 1, dtype=torch.float32, device="cuda")
+    xd = raw[1:]
+    xd.copy_(torch.from_numpy(x.reshape(-1)))
+    s = e.empty_spectral()
+    gbfft.check(gbfft.lib().gbfft_exec_r2c(e.h, xd.data_ptr(), s.data_ptr(), None))
+    ref = O.fft3d_r2c(x.astype(np.float64), fmt)
+    assert rel(s.cpu().numpy(), ref) <= TOL["s"]
+    out_raw = torch.zeros(nx * ny * nz + 1, dtype=torch.float32, device="cuda")
+    gbfft.check(gbfft.lib().gbfft_exec_c2r(e.h, s.data_ptr(), out_raw[1:].data_ptr(), None))
+    torch.cuda.synchronize()
+    back = out_raw[1:].cpu().numpy().reshape(nz, ny, nx) / (nx * ny * nz)
+    assert np.allclose(back, x, atol=1e-5)
+    e.close()
