@@ -125,12 +125,14 @@ std::vector<double> twiddles(int n) {
 // Stage-major twiddles of the power-of-two kernel: stage s of radix R after
 // NS points holds W_{NS R}^{k r} at (NS - 1) + (r - 1) NS + k, for
 // r = 1..R-1, k = 0..NS-1 (n - 1 entries in all).
-std::vector<double> stage_twiddles(int n, int e) {
+std::vector<double> stage_twiddles(const std::vector<int>& radices) {
+  int n = 1;
+  for (int r : radices) n *= r;
   std::vector<double> t(2 * (size_t)n, 0.0);
   const long double two_pi = 6.283185307179586476925286766559005768L;
   int ns = 1;
-  for (int s = 0; s < fast_nst(n, e); ++s) {
-    const int R = fast_radix(n, e, s);
+  for (size_t s = 0; s < radices.size(); ++s) {
+    const int R = radices[s];
     for (int r = 1; r < R; ++r)
       for (int k = 0; k < ns; ++k) {
         const long long m = ((long long)k * r) % ((long long)ns * R);
@@ -164,7 +166,14 @@ int upload_table(void** dst, const std::vector<double>& t, int prec) {
 
 int upload_twiddles(AxisPlan& p, int prec) {
   int rc = upload_table(&p.d_tw, twiddles(p.n), prec);
-  if (rc == GBFFT_OK && fast_length(p.n)) rc = upload_table(&p.d_twf, stage_twiddles(p.n, p.fast_e), prec);
+  if (rc == GBFFT_OK && fast_length(p.n)) {
+    std::vector<int> radices;
+    for (int s = 0; s < fast_nst(p.n, p.fast_e); ++s) radices.push_back(fast_radix(p.n, p.fast_e, s));
+    rc = upload_table(&p.d_twf, stage_twiddles(radices), prec);
+  } else if (rc == GBFFT_OK && mixed_length(p.n)) {
+    const int r0 = mixed_r0(p.n);
+    rc = upload_table(&p.d_twf, stage_twiddles({r0, p.n / r0}), prec);
+  }
   return rc;
 }
 
@@ -293,7 +302,35 @@ int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int f
 }
 
 // Fill the plan-dependent fields of a pass.
+// Lines per CTA for the mixed-radix kernel (R1 = n / mixed_r0(n) threads a
+// line, at most 256 threads a CTA).
+int mixed_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int forced_L) {
+  const int tpl = n / mixed_r0(n);
+  if (forced_L > 0) return forced_L;
+  int L = contiguous ? 192 / tpl : 256 / tpl;
+  if (!contiguous) {
+    const int min_l = (int)(64 / (2 * prec));
+    if (L < min_l) L = min_l;
+  }
+  while (L > 1 && L * tpl > 256) --L;
+  while (L > 1 && (size_t)fast_smem_entries(n, L) * 2 * prec > 100 * 1024) --L;
+  if (L < 1) L = 1;
+  if (L > 1 && nlines < L) L = (int)nlines;
+  return L;
+}
+
 void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind, int forced_L) {
+  if (mixed_length(p.n)) {
+    a.n = p.n;
+    a.nst = 0;
+    a.tw = p.d_twf;
+    a.fast = 2;
+    a.tpl = p.n / mixed_r0(p.n);
+    a.L = mixed_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L);
+    a.first_fused = 1;
+    a.last_fused = kind != K_R2C;
+    return;
+  }
   if (fast_length(p.n)) {
     a.n = p.n;
     a.nst = 0;
@@ -789,6 +826,14 @@ int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
   else
     axis = kind - GBFFT_PASS_C2C_X;
   const AxisPlan& p = e->ax[axis];
+  if (mixed_length(p.n)) {
+    const int tpl_m = p.n / mixed_r0(p.n);
+    if (lines * tpl_m > 256) return fail(GBFFT_ERR_INVALID, "tile exceeds the kernel's thread limit");
+    if ((size_t)fast_smem_entries(p.n, lines) * 2 * (size_t)e->prec > 200 * 1024)
+      return fail(GBFFT_ERR_INVALID, "tile exceeds the shared-memory limit");
+    e->tile_L[kind] = lines;
+    return GBFFT_OK;
+  }
   const bool fast = fast_length(p.n);
   const bool contig_pass = (kind == GBFFT_PASS_C2C_X) ||
                            ((kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R) &&

@@ -54,7 +54,7 @@ struct PassArgs {
   int nv;          // strided: extent of v (grid.y)
   int first_fused; // stage 0 reads global memory directly
   int last_fused;  // last stage writes global memory directly
-  int fast;        // 1: run the compile-time power-of-two kernel for n
+  int fast;        // 1: compile-time power-of-two kernel, 2: mixed-radix kernel
   int pair_vec;    // r2c/c2r on strided lines: the two real lines of a pair
                    // are adjacent and 8-byte aligned (read/write as one pair)
   int radix[kMaxStages];
@@ -81,6 +81,21 @@ __host__ __device__ constexpr int fast_radix(int n, int e, int s) {
 }
 constexpr int kFastMaxThreadsF32 = 512;
 constexpr int kFastMaxThreadsF64 = 256;
+// Mixed-radix lengths with a compile-time-planned kernel (fft_mixed.cuh):
+// n = R0 * R1, R0 <= R1 <= 32, the most balanced such split.
+__host__ __device__ constexpr int mixed_r0(int n) {
+  int best = 0;
+  for (int a = 2; a <= 32; ++a)
+    if (n % a == 0 && n / a <= 32 && a <= n / a) best = a;
+  return best;
+}
+__host__ __device__ constexpr bool mixed_length(int n) {
+  return n == 48 || n == 96 || n == 192 || n == 210 || n == 243 || n == 270 || n == 360 ||
+         n == 384 || n == 400;
+}
+cudaError_t launch_mixed_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+cudaError_t launch_mixed_f64(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+
 // Thread limit of the power-of-two kernel for E points a thread.
 __host__ __device__ constexpr int fast_max_threads(int e, int prec_bytes) {
   return e == 32 ? 256 : (prec_bytes == 4 ? kFastMaxThreadsF32 : kFastMaxThreadsF64);

@@ -346,3 +346,45 @@ def test_real_array_at_odd_element_offset(fmt):
     back = out_raw[1:].cpu().numpy().reshape(nz, ny, nx) / (nx * ny * nz)
     assert np.allclose(back, x, atol=1e-5)
     e.close()
+
+
+# Mixed-radix lengths with compile-time kernels (48, 96, 192, 210, 243, 270,
+# 360, 384, 400) on every axis, both formats, both precisions.
+MIXED_SHAPES = [(384, 400, 6), (360, 270, 4), (243, 210, 5), (48, 96, 192), (192, 48, 96),
+                (210, 3, 243), (400, 2, 384), (270, 360, 2)]
+
+
+@pytest.mark.parametrize("prec", ["d", "s"])
+@pytest.mark.parametrize("fmt", [O.PHYSICAL_IN_X, O.PHYSICAL_IN_Z])
+@pytest.mark.parametrize("shape", MIXED_SHAPES)
+def test_mixed_radix_against_oracle(gpu, prec, fmt, shape):
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx + 3 * ny + 7 * nz + fmt)
+    x = rng.uniform(-1, 1, (nz, ny, nx))
+    rt = np.float64 if prec == "d" else np.float32
+    ct = np.complex128 if prec == "d" else np.complex64
+    ref = O.fft3d_r2c(x, fmt)
+    assert rel(gpu[prec].r2c(x.astype(rt), fmt, None), ref) <= TOL[prec]
+    s = ref + 0.2 * (rng.standard_normal(ref.shape) + 1j * rng.standard_normal(ref.shape))
+    assert rel(gpu[prec].c2r(s.astype(ct), nx, ny, nz, fmt, False, None),
+               O.fft3d_c2r(s.copy(), nx, ny, nz, fmt)) <= TOL[prec]
+    c = x + 1j * rng.uniform(-1, 1, x.shape)
+    for isign in (O.FORWARD, O.BACKWARD):
+        assert rel(gpu[prec].c2c(c.astype(ct), fmt, isign, False, None),
+                   O.fft3d_c2c(c.copy(), fmt, isign)) <= TOL[prec]
+
+
+@pytest.mark.parametrize("shape", [(384, 400, 243), (360, 270, 210)])
+@pytest.mark.parametrize("prec", ["d", "s"])
+def test_full_size_mixed_grids(gpu, shape, prec):
+    # the non-power-of-two grids at full size: forward spectrum against the
+    # FP64 oracle and the r2c -> c2r round trip
+    nx, ny, nz = shape
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, (nz, ny, nx))
+    rt = np.float64 if prec == "d" else np.float32
+    s = gpu[prec].r2c(x.astype(rt), O.PHYSICAL_IN_X, None)
+    ref = O.fft3d_r2c(x, O.PHYSICAL_IN_X)
+    assert rel(s, ref) <= TOL[prec]
+    y = gpu[prec].c2r(s, nx, ny, nz, O.PHYSICAL_IN_X, False, None) / (nx * ny * nz)
+    assert rel(y, x) <= (1e-13 if prec == "d" else 1e-6)
