@@ -538,6 +538,60 @@ void warn_skip(int code) {
 
 }  // namespace
 
+namespace {
+
+// The passes of a 3D r2c (src/fft_common_3d.f90:121-189): the r2c pass
+// along the real axis into `out`, then the c2c passes on `out`.
+std::vector<Pass> r2c_passes(gbfft_engine_s* e, const void* d_in, void* d_out) {
+  std::vector<Pass> ps;
+  const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
+  ps.push_back(real_pass(e, K_R2C, d_in, d_out));
+  if (e->format == GBFFT_PHYSICAL_IN_X) {
+    if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
+    if (!e->skip[2]) ps.push_back(c2c_pass(e, 2, s1, s2, s3, d_out, d_out, 0));
+  } else {
+    if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
+    if (!e->skip[0]) ps.push_back(c2c_pass(e, 0, s1, s2, s3, d_out, d_out, 0));
+  }
+  return ps;
+}
+
+// The passes of a 3D c2r (src/fft_common_3d.f90:194-296): c2c passes into
+// the work array W (the input itself when OVERWRITE), then the c2r pass.
+std::vector<Pass> c2r_passes(gbfft_engine_s* e, void* d_in, void* d_out) {
+  std::vector<Pass> ps;
+  void* W = e->inplace ? d_in : e->work;
+  const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
+  const void* cur = d_in;
+  const int order_x[2] = {2, 1};  // PHYSICAL_IN_X: z then y, then c2r along x
+  const int order_z[2] = {0, 1};  // PHYSICAL_IN_Z: x then y, then c2r along z
+  const int* order = e->format == GBFFT_PHYSICAL_IN_X ? order_x : order_z;
+  for (int i = 0; i < 2; ++i) {
+    const int ax = order[i];
+    if (e->skip[ax]) continue;
+    ps.push_back(c2c_pass(e, ax, s1, s2, s3, cur, W, 1));
+    cur = W;
+  }
+  ps.push_back(real_pass(e, K_C2R, cur, d_out));
+  return ps;
+}
+
+}  // namespace
+
+int gbfft::engine_passes(gbfft_engine_s* e, int which, const void* in, void* out, PassInfo* out_passes,
+                         int max_passes, int* n) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (which == 1 && !(e->inplace ? in : e->work)) return fail(GBFFT_ERR_STATE, "engine has no work area");
+  std::vector<Pass> ps =
+      which == 0 ? r2c_passes(e, in, out) : c2r_passes(e, const_cast<void*>(in), out);
+  if ((int)ps.size() > max_passes) return fail(GBFFT_ERR_INVALID, "too many passes");
+  for (size_t i = 0; i < ps.size(); ++i) out_passes[i] = PassInfo{ps[i].a, ps[i].kind, ps[i].contiguous};
+  *n = (int)ps.size();
+  return GBFFT_OK;
+}
+
+int gbfft::engine_precision(gbfft_engine_s* e) { return valid_engine(e) ? e->prec : 0; }
+
 int gbfft::set_error(int code, const char* msg) {
   g_err = msg ? msg : "";
   return code;
@@ -701,20 +755,10 @@ int gbfft_exec_r2c(gbfft_engine_t e, const void* d_in, void* d_out, void* stream
   if (!aligned(d_in, e->prec) || !aligned(d_out, cbytes(e)))
     return fail(GBFFT_ERR_INVALID, "array not aligned to its element size");
   cudaStream_t st = (cudaStream_t)stream;
-  std::vector<Pass> ps;
-  const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
-  if (e->format == GBFFT_PHYSICAL_IN_X) {
-    if (e->skip[0]) warn_skip(1);
-    ps.push_back(real_pass(e, K_R2C, d_in, d_out));
-    if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
-    if (!e->skip[2]) ps.push_back(c2c_pass(e, 2, s1, s2, s3, d_out, d_out, 0));
-  } else {
-    if (e->skip[2]) warn_skip(2);
-    ps.push_back(real_pass(e, K_R2C, d_in, d_out));
-    if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
-    if (!e->skip[0]) ps.push_back(c2c_pass(e, 0, s1, s2, s3, d_out, d_out, 0));
-  }
-  if (e->fuse) fuse_xy(e, ps, s3);
+  if ((e->format == GBFFT_PHYSICAL_IN_X && e->skip[0]) || (e->format == GBFFT_PHYSICAL_IN_Z && e->skip[2]))
+    warn_skip(e->format == GBFFT_PHYSICAL_IN_X ? 1 : 2);
+  std::vector<Pass> ps = r2c_passes(e, d_in, d_out);
+  if (e->fuse) fuse_xy(e, ps, e->sp[2]);
   return run_passes(e, ps, st);
 }
 
@@ -728,25 +772,11 @@ int gbfft_exec_c2r(gbfft_engine_t e, void* d_in, void* d_out, void* stream) {
   if (!aligned(d_in, cbytes(e)) || !aligned(d_out, e->prec))
     return fail(GBFFT_ERR_INVALID, "array not aligned to its element size");
   cudaStream_t st = (cudaStream_t)stream;
-  void* W = e->inplace ? d_in : e->work;
-  if (!W) return fail(GBFFT_ERR_STATE, "engine has no work area");
-  const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
-  std::vector<Pass> ps;
-  const void* cur = d_in;
-  // c2c passes in the reference's order (src/fft_common_3d.f90:216-283)
-  const int order_x[2] = {2, 1};  // PHYSICAL_IN_X: z then y, then c2r along x
-  const int order_z[2] = {0, 1};  // PHYSICAL_IN_Z: x then y, then c2r along z
-  const int* order = e->format == GBFFT_PHYSICAL_IN_X ? order_x : order_z;
-  for (int i = 0; i < 2; ++i) {
-    const int ax = order[i];
-    if (e->skip[ax]) continue;
-    ps.push_back(c2c_pass(e, ax, s1, s2, s3, cur, W, 1));
-    cur = W;
-  }
+  if (!(e->inplace ? d_in : e->work)) return fail(GBFFT_ERR_STATE, "engine has no work area");
   if (e->format == GBFFT_PHYSICAL_IN_X && e->skip[0]) warn_skip(3);
   if (e->format == GBFFT_PHYSICAL_IN_Z && e->skip[2]) warn_skip(4);
-  ps.push_back(real_pass(e, K_C2R, cur, d_out));
-  if (e->fuse) fuse_xy(e, ps, s3);
+  std::vector<Pass> ps = c2r_passes(e, d_in, d_out);
+  if (e->fuse) fuse_xy(e, ps, e->sp[2]);
   return run_passes(e, ps, st);
 }
 

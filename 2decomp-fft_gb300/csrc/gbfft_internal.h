@@ -7,6 +7,8 @@
 #include <cstddef>
 #include <cstdint>
 
+struct gbfft_engine_s;
+
 namespace gbfft {
 
 constexpr int kMaxStages = 16;    // radix stages of one axis plan
@@ -128,6 +130,34 @@ bool fused_supported(int prec_bytes, int kindx, bool x_first, int nx, int ny);
 constexpr int kFusedThreads = 512;
 // Enqueue a fused x/y pass (zeroes f.sync first).
 cudaError_t launch_fused(int prec_bytes, int kindx, bool x_first, const FusedArgs& f, cudaStream_t stream);
+
+// ---- batches: every pass of many grids in one persistent launch ----------
+constexpr int kBatchThreads = 256;
+struct BatchDesc {
+  PassArgs a;       // a.L = tile lines + 1 (shared-memory layout lines)
+  int code;         // 2 * kind + (strided ? 1 : 0)
+  int dep;          // descriptor that must be complete first, or -1
+  long long lines;  // complex lines of the pass (contiguous) or nu * nv (strided)
+  long long nu;     // strided: lines along u (x)
+};
+// Line lengths the batch kernel runs: 32, 48, 64, 96, 128, 192, 256.
+bool batch_length(int n);
+// Lines one 256-thread tile holds for a length and contiguity.
+int batch_tile_lines(int n, bool contiguous);
+cudaError_t launch_batch_f32(const BatchDesc* d_desc, const long long* d_prefix, int ndesc, int* d_sync,
+                             long long sync_ints, cudaStream_t stream);
+
+// The unfused passes an engine would run for r2c (which = 0) or c2r
+// (which = 1) between the given arrays (the engine's pipeline, without
+// launching anything).
+struct PassInfo {
+  PassArgs a;
+  int kind;
+  bool contiguous;
+};
+int engine_precision(struct ::gbfft_engine_s* e);
+int engine_passes(struct ::gbfft_engine_s* e, int which, const void* in, void* out, PassInfo* out_passes,
+                  int max_passes, int* n);
 
 // Shared memory the runtime-planned pass needs for L lines of length n
 // (two padded buffers); the power-of-two pass needs half of it.

@@ -55,6 +55,10 @@ SIGNATURES = {
     "gbfft_batch_add": (_i, [_vp, _vp, _vp, _vp]),
     "gbfft_batch_forward": (_i, [_vp, _vp]),
     "gbfft_batch_backward": (_i, [_vp, _vp]),
+    "gbfft_batch_set_persistent": (_i, [_vp, _i]),
+    "gbfft_batch_run": (_i, [_vp, _i, _vp]),
+    "gbfft_batch_info": (_i, [_vp, _ip, _ip]),
+    "gbfft_batch_status": (_i, [_vp]),
     "gbfft_batch_graph_build": (_i, [_vp, _vp]),
     "gbfft_batch_graph_launch": (_i, [_vp, _vp]),
     "gbfft_batch_destroy": (_i, [_vp]),
@@ -284,6 +288,20 @@ class Batch:
 
     def backward(self, stream=None):
         check(lib().gbfft_batch_backward(self.h, _stream(stream)))
+
+    def set_persistent(self, enable):
+        check(lib().gbfft_batch_set_persistent(self.h, int(bool(enable))))
+
+    def run(self, mask=3, stream=None):
+        check(lib().gbfft_batch_run(self.h, int(mask), _stream(stream)))
+
+    def info(self):
+        p, n = ctypes.c_int(), ctypes.c_int()
+        check(lib().gbfft_batch_info(self.h, ctypes.byref(p), ctypes.byref(n)))
+        return {"persistent": bool(p.value), "launches_per_run": n.value}
+
+    def status(self):
+        check(lib().gbfft_batch_status(self.h))
 
     def graph_build(self, stream):
         check(lib().gbfft_batch_graph_build(self.h, _stream(stream)))

@@ -50,6 +50,7 @@ WORKLOADS = {
     "r2c_c2r_1024x64x512_f32_x": (1024, 64, 512, 1, 4, "gauss_modes"),
 }
 DEFAULT_WORKLOAD = "r2c_c2r_1024x1024x512_f32_x"
+BATCH_WORKLOAD = "batched_64_grids_f32"
 
 
 # ---------------------------------------------------------------------------
@@ -436,6 +437,112 @@ def run_gb300(args):
     return out
 
 
+def batch_dims(count=64, seed=6):
+    """64 grids, each dimension drawn from {32,48,64,96,128,192,256} (seed 6),
+    PHYSICAL_IN_X or PHYSICAL_IN_Z by a seeded coin."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        nx, ny, nz = (int(v) for v in rng.choice([32, 48, 64, 96, 128, 192, 256], size=3))
+        fmt = 1 if rng.random() < 0.5 else 3
+        out.append((nx, ny, nz, fmt))
+    return out
+
+
+def run_batched(args):
+    """Batched uneven grids: forward + backward of 64 FP32 grids per step,
+    timed as one persistent launch replayed from a CUDA graph (value) and as
+    the per-grid launch loop (reported beside it)."""
+    import numpy as np
+    import torch
+    import gbfft
+    world, rank, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    gbfft.lib()
+    dims = batch_dims()
+    rng = np.random.default_rng(7)
+    items = []
+    batch = gbfft.Batch()
+    npts = 0
+    for nx, ny, nz, fmt in dims:
+        e = gbfft.Engine(fmt, nx, ny, nz, prec=gbfft.PREC_SINGLE)
+        x = torch.from_numpy(rng.uniform(-1, 1, (nz, ny, nx)).astype(np.float32)).to(dev)
+        s = e.empty_spectral(device=dev)
+        batch.add(e, x, s)
+        items.append((e, x, s, fmt))
+        npts += nx * ny * nz
+    stream = torch.cuda.Stream(dev)
+    info = batch.info()
+    # per-grid error of the forward spectrum against FP64 (before timing)
+    x0 = [x.clone() for _, x, _, _ in items]
+    batch.run(1, stream)
+    stream.synchronize()
+    errs = []
+    for (e, x, s, fmt) in items:
+        xd = x.double().cpu().numpy()
+        ref = np.fft.rfftn(xd, axes=(0, 1, 2)) if fmt == 1 else np.fft.rfftn(xd, axes=(2, 1, 0))
+        errs.append(float(np.linalg.norm(s.cpu().numpy() - ref) / np.linalg.norm(ref)))
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = gbfft.launch_count()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / steps, gbfft.launch_count() - l0
+
+    batch.graph_build(stream)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    t0 = time.time()
+    ms_graph, _ = timed(lambda: batch.graph_launch(stream), args.steps, args.warmup)
+    t1 = time.time()
+    # kernels per step: one persistent launch, or every pass of every grid
+    l0 = gbfft.launch_count()
+    batch.run(3, stream)
+    stream.synchronize()
+    per_step = gbfft.launch_count() - l0
+    launches = per_step * args.steps
+    batch.status()
+    batch.set_persistent(False)
+    batch.graph_build(stream)
+    ms_loop_graph, _ = timed(lambda: batch.graph_launch(stream), args.steps, args.warmup)
+    ms_loop, loop_launches = timed(lambda: (batch.forward(stream), batch.backward(stream)), args.steps,
+                                   args.warmup)
+    for (e, x, s, fmt), xr in zip(items, x0):
+        x.copy_(xr)
+    clocks.stop()
+    for (e, x, s, fmt), xr in zip(items, x0):
+        x.copy_(xr)
+    value = npts / (ms_graph * 1e-3) / 1e9
+    out = {"metric": METRIC, "value": round(value, 3), "unit": "GPts/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_graph, 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic: seeded uniform [-1,1)",
+           "config": {"workload": "batched uneven grids: 64 FP32 grids, dims from {32..256}, mixed X/Z, "
+                                  "r2c+c2r per step", "name": BATCH_WORKLOAD, "points": npts,
+                      "persistent": info["persistent"],
+                      "l2": "no flush (total working set %.0f MB)" % (npts * 4 * 3 / 1e6)},
+           "batch": {"persistent_graph_ms": round(ms_graph, 4), "per_grid_loop_graph_ms": round(ms_loop_graph, 4),
+                     "per_grid_loop_ms": round(ms_loop, 4), "launches_per_step_persistent": per_step,
+                     "launches_per_step_loop": loop_launches / args.steps,
+                     "speedup_vs_loop": round(ms_loop / ms_graph, 3),
+                     "per_grid_rel_l2_vs_fp64_max": max(errs), "per_grid_rel_l2_vs_fp64_median": sorted(errs)[len(errs) // 2]},
+           "gpu_launches": int(launches), "clocks": clocks.summary(t0, t1)}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    batch.close()
+    return out
+
+
 def read_traffic(workload, kernel):
     """DRAM bytes per launch of `kernel` from the committed ncu summary
     (profiles/dram_traffic.txt: `workload kernel bytes_per_launch`)."""
@@ -486,7 +593,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [BATCH_WORKLOAD])
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -496,6 +603,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == BATCH_WORKLOAD:
+        run_batched(args)
     else:
         run_gb300(args)
 

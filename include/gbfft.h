@@ -124,16 +124,33 @@ int gbfft_warning_count(void);
  *      src/fft_common.f90:381-479) ------------------------------------- */
 typedef struct gbfft_batch_s* gbfft_batch_t;
 
-/* A batch groups engines of the same precision and plain form.  Each item
- * is one engine with its own input and output; gbfft_batch_forward runs every
- * item's r2c, gbfft_batch_backward every item's c2r. */
+/* A batch is a list of (engine, real array, spectral array) items.  Forward
+ * runs every item's r2c (real -> spectral), backward every item's c2r
+ * (spectral -> real, the real array is overwritten).
+ *   gbfft_batch_forward / _backward   per-grid loop: each grid's passes as
+ *                                     their own launches, grid after grid;
+ *   gbfft_batch_run(mask)             mask 1 forward, 2 backward, 3 both:
+ *                                     in ONE persistent launch when the batch
+ *                                     is persistent-capable (FP32 engines,
+ *                                     every line length in 32, 48, 64, 96,
+ *                                     128, 192, 256), else the per-grid loop.
+ * gbfft_batch_set_persistent(0) forces the per-grid loop.  The persistent
+ * launch uploads its pass descriptors on first use (synchronously). */
 int gbfft_batch_create(gbfft_batch_t* batch);
 int gbfft_batch_add(gbfft_batch_t batch, gbfft_engine_t engine,
                     const void* d_real, void* d_spec);
 int gbfft_batch_forward(gbfft_batch_t batch, void* stream);
 int gbfft_batch_backward(gbfft_batch_t batch, void* stream);
-/* Capture forward then backward of the whole batch in one CUDA graph and
- * replay it: gbfft_batch_graph_launch enqueues the replay on `stream`. */
+int gbfft_batch_set_persistent(gbfft_batch_t batch, int enable);
+int gbfft_batch_run(gbfft_batch_t batch, int mask, void* stream);
+/* persistent = 1 when gbfft_batch_run uses the one-launch path. */
+int gbfft_batch_info(gbfft_batch_t batch, int* persistent, int* launches_per_run);
+/* Status of the last persistent run (waits for the device): GBFFT_ERR_TIMEOUT
+ * if one of its bounded inter-tile waits gave up. */
+int gbfft_batch_status(gbfft_batch_t batch);
+/* Capture gbfft_batch_run(batch, 3) (forward then backward, persistent or
+ * per-grid loop as set) in one CUDA graph; gbfft_batch_graph_launch enqueues
+ * a replay on `stream`.  Capture needs a non-default stream. */
 int gbfft_batch_graph_build(gbfft_batch_t batch, void* stream);
 int gbfft_batch_graph_launch(gbfft_batch_t batch, void* stream);
 int gbfft_batch_destroy(gbfft_batch_t batch);
