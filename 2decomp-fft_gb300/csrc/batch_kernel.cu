@@ -17,9 +17,8 @@
 // line length: power-of-two lengths 32..256 and the mixed lengths 48, 96,
 // 192.  Strided passes flatten their (u, v) lines so that small grids fill a
 // tile.
-#include <cuda/atomic>
-
 #include "fft_fast.cuh"
+#include "fft_sync.cuh"
 #include "fft_mixed.cuh"
 #include "gbfft_internal.h"
 
@@ -117,18 +116,8 @@ __global__ void __launch_bounds__(kBT, 4)
     const BatchDesc& D = desc[lo];
     const long long tile = tk - prefix[lo];
     if (D.dep >= 0) {
-      if (threadIdx.x == 0) {
-        cuda::atomic_ref<int, cuda::thread_scope_device> done(sync[2 + D.dep]);
-        const int need = (int)(prefix[D.dep + 1] - prefix[D.dep]);
-        long long polls = 0;
-        while (done.load(cuda::memory_order_acquire) < need) {
-          if (++polls > kSpinLimit) {
-            atomicExch(sync + 1, 1);
-            break;
-          }
-          __nanosleep(64);
-        }
-      }
+      if (threadIdx.x == 0)
+        bounded_wait(sync + 2 + D.dep, (int)(prefix[D.dep + 1] - prefix[D.dep]), kSpinLimit, sync + 1, 1);
       __syncthreads();
     }
     bool ok;
@@ -149,7 +138,19 @@ __global__ void __launch_bounds__(kBT, 4)
 
 int g_grid = 0;
 
+// One thread waits for counter[0] >= need with a poll limit (self-test of
+// the bounded wait).
+__global__ void wait_selftest_kernel(int* words, int need, long long limit) {
+  if (threadIdx.x == 0) bounded_wait(words, need, limit, words + 1, 1);
+}
+
 }  // namespace
+
+cudaError_t launch_wait_selftest(int* d_words, int need, long long limit, cudaStream_t stream) {
+  wait_selftest_kernel<<<1, 32, 0, stream>>>(d_words, need, limit);
+  add_launches(1);
+  return cudaGetLastError();
+}
 
 bool batch_length(int n) {
   return n == 32 || n == 48 || n == 64 || n == 96 || n == 128 || n == 192 || n == 256;

@@ -896,6 +896,21 @@ int gbfft_engine_status(gbfft_engine_t e) {
   return GBFFT_OK;
 }
 
+int gbfft_selftest_bounded_wait(int counter_value, int need, long long poll_limit, int* timed_out) {
+  if (!timed_out || poll_limit < 1 || poll_limit > (1ll << 26)) return fail(GBFFT_ERR_INVALID, "bad argument");
+  int* d = nullptr;
+  cudaError_t err = cudaMalloc(&d, 2 * sizeof(int));
+  if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc");
+  int h[2] = {counter_value, 0};
+  err = cudaMemcpy(d, h, sizeof h, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = launch_wait_selftest(d, need, poll_limit, nullptr);
+  if (err == cudaSuccess) err = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (err != cudaSuccess) return cuda_fail(err, "bounded-wait self-test");
+  *timed_out = h[1];
+  return GBFFT_OK;
+}
+
 int gbfft_engine_set_fusion(gbfft_engine_t e, int enable) {
   if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
   e->fuse = enable != 0;

@@ -27,9 +27,8 @@
 // With LAG = 2 about five planes are in flight, a few MB of L2.
 #pragma once
 
-#include <cuda/atomic>
-
 #include "fft_fast.cuh"
+#include "fft_sync.cuh"
 
 namespace gbfft {
 namespace fused {
@@ -121,17 +120,7 @@ __global__ void __launch_bounds__(kThreads, 1) fused_xy_kernel(const __grid_cons
       __syncthreads();
       if (threadIdx.x == 0) atomicAdd(sync + 2 + plane, 1);
     } else {
-      if (threadIdx.x == 0) {
-        cuda::atomic_ref<int, cuda::thread_scope_device> done(sync[2 + plane]);
-        long long polls = 0;
-        while (done.load(cuda::memory_order_acquire) < n1) {
-          if (++polls > kSpinLimit) {
-            atomicExch(sync + 1, 1);
-            break;
-          }
-          __nanosleep(64);
-        }
-      }
+      if (threadIdx.x == 0) bounded_wait(sync + 2 + plane, n1, kSpinLimit, sync + 1, 1);
       __syncthreads();
       if constexpr (XFIRST)
         y_tile<T, true, NY>(f.ay, Sm, plane, item);

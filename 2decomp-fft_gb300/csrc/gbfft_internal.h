@@ -147,6 +147,10 @@ int batch_tile_lines(int n, bool contiguous);
 cudaError_t launch_batch_f32(const BatchDesc* d_desc, const long long* d_prefix, int ndesc, int* d_sync,
                              long long sync_ints, cudaStream_t stream);
 
+// Self-test of the bounded inter-CTA wait: d_words[0] is the counter,
+// d_words[1] receives 1 when the wait gave up.
+cudaError_t launch_wait_selftest(int* d_words, int need, long long limit, cudaStream_t stream);
+
 // The unfused passes an engine would run for r2c (which = 0) or c2r
 // (which = 1) between the given arrays (the engine's pipeline, without
 // launching anything).

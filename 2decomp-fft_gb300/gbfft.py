@@ -69,6 +69,7 @@ SIGNATURES = {
     "gbfft_engine_profile_read": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "gbfft_exec_c2r_noalloc": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "gbfft_selftest_bounded_wait": (_i, [_i, _i, ctypes.c_longlong, _ip]),
     "gbfft_version": (_i, [_ip, _ip]),
     "gbfft_launch_count": (ctypes.c_longlong, []),
     # decomp_2d_fft.h

@@ -208,6 +208,13 @@ int gbfft_engine_profile_read(gbfft_engine_t engine, int kind, long long* launch
 int gbfft_exec_c2r_noalloc(int format, int nx, int ny, int nz, int prec,
                            const void* d_in, void* d_out, void* stream);
 
+/* Failure detection self-test (no counterpart in the reference): run the
+ * bounded wait the inter-CTA kernels use, on a device counter holding
+ * counter_value, waiting for `need` with at most poll_limit polls (<= 2^26).
+ * *timed_out = 1 when the wait gave up (counter_value < need), 0 otherwise.
+ * The kernel ends either way; nothing is left waiting on the GPU. */
+int gbfft_selftest_bounded_wait(int counter_value, int need, long long poll_limit, int* timed_out);
+
 /* Library version and kernel-launch counter (every kernel this library has
  * enqueued since load), for benchmarks that report launches. */
 int gbfft_version(int* major, int* minor);
