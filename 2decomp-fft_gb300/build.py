@@ -65,7 +65,7 @@ def build(force=False, verbose=False, extra=()):
             if log.strip():
                 print(log)
     tmp = LIB + ".tmp.%d" % os.getpid()
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results] + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))

@@ -12,8 +12,13 @@
 //   c2c:  in -> out -> out -> out              (in is never modified)
 //   c2r:  in -> W -> W -> out, W = in when inplace, else the engine's work
 //         area (the complex intermediate does not fit in the real output).
+#include <dlfcn.h>
+
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
+#include <fstream>
+#include <sstream>
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
@@ -177,6 +182,76 @@ int upload_twiddles(AxisPlan& p, int prec) {
   return rc;
 }
 
+// ---- tuning cache -------------------------------------------------------
+// Text file, one shape per line:
+//   prec format nx ny nz key=value ...
+// keys: r2c c2r c2c_x c2c_y c2c_z xy_fused (lines per CTA of that pass),
+// fuse (0/1), e_y e_z (points per thread of the strided y / z plan).
+struct TuneEntry {
+  int prec = 0, format = 0, nx = 0, ny = 0, nz = 0;
+  int fuse = -1;
+  int L[GBFFT_PASS_KINDS] = {0};
+  int e[3] = {0, 0, 0};
+};
+
+std::mutex g_tune_mu;
+bool g_tune_loaded = false;
+std::string g_tune_path_override;
+bool g_tune_path_set = false;
+std::vector<TuneEntry> g_tune;
+
+std::string default_tune_path() {
+  const char* env = std::getenv("GBFFT_TUNE_CACHE");
+  if (env) return env;
+  Dl_info info;
+  if (dladdr(reinterpret_cast<void*>(&gbfft_engine_create), &info) && info.dli_fname) {
+    std::string so = info.dli_fname;  // .../2decomp-fft_gb300/lib/libgbfft.so
+    size_t a = so.rfind('/');
+    if (a != std::string::npos) {
+      size_t b = so.rfind('/', a == 0 ? 0 : a - 1);
+      if (b != std::string::npos) return so.substr(0, b) + "/tune_cache.txt";
+    }
+  }
+  return "";
+}
+
+void load_tune_locked() {
+  g_tune.clear();
+  g_tune_loaded = true;
+  const std::string path = g_tune_path_set ? g_tune_path_override : default_tune_path();
+  if (path.empty()) return;
+  std::ifstream f(path);
+  std::string line;
+  static const char* names[GBFFT_PASS_KINDS] = {"r2c", "c2r", "c2c_x", "c2c_y", "c2c_z", "xy_fused"};
+  while (std::getline(f, line)) {
+    if (line.empty() || line[0] == '#') continue;
+    std::istringstream in(line);
+    TuneEntry t;
+    if (!(in >> t.prec >> t.format >> t.nx >> t.ny >> t.nz)) continue;
+    std::string kv;
+    while (in >> kv) {
+      const size_t eq = kv.find('=');
+      if (eq == std::string::npos) continue;
+      const std::string k = kv.substr(0, eq);
+      const int v = std::atoi(kv.c_str() + eq + 1);
+      if (k == "fuse") t.fuse = v;
+      else if (k == "e_y") t.e[1] = v;
+      else if (k == "e_z") t.e[2] = v;
+      for (int i = 0; i < GBFFT_PASS_KINDS; ++i)
+        if (k == names[i]) t.L[i] = v;
+    }
+    g_tune.push_back(t);
+  }
+}
+
+TuneEntry lookup_tune(int prec, int format, int nx, int ny, int nz) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (!g_tune_loaded) load_tune_locked();
+  for (const TuneEntry& t : g_tune)
+    if (t.prec == prec && t.format == format && t.nx == nx && t.ny == ny && t.nz == nz) return t;
+  return TuneEntry();
+}
+
 }  // namespace
 
 struct ProfRec {
@@ -273,8 +348,7 @@ int lines_per_cta(const AxisPlan& p, int prec, bool contiguous, long long nlines
 
 // Lines per CTA for the power-of-two kernel (n / fast_points(n) threads per
 // line).
-int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int forced_L) {
-  const int e = fast_points(n, contiguous);
+int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int forced_L, int e) {
   const int tpl = n / e;
   if (forced_L > 0) return forced_L;
   const int maxt = fast_max_threads(e, prec);
@@ -336,8 +410,9 @@ void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int ki
     a.nst = 0;
     a.tw = p.d_twf;
     a.fast = 1;
-    a.tpl = p.n / fast_points(p.n, contiguous);
-    a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L);
+    const int fe = contiguous ? fast_points(p.n, true) : p.fast_e;
+    a.tpl = p.n / fe;
+    a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L, fe);
     a.first_fused = 1;
     a.last_fused = kind != K_R2C;
     (void)kind;
@@ -470,6 +545,7 @@ void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
     Pass& py = xfirst ? p1 : p0;
     if (p1.a.src != p0.a.dst) continue;
     if (!fast_length(px.a.n) || !fast_length(py.a.n)) continue;
+    if (e->ax[1].fast_e != fast_points(py.a.n, false)) continue;  // the fused kernel's y plan
     if (!fused_supported(e->prec, px.kind, xfirst, px.a.n, py.a.n)) continue;
     long long per_plane;
     if (px.kind == K_C2C) {
@@ -672,6 +748,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
   e->sp[1] = ny;
   e->sp[2] = format == GBFFT_PHYSICAL_IN_Z ? nz / 2 + 1 : nz;
 
+  const TuneEntry tune = lookup_tune(prec, format, nx, ny, nz);
   const int lens[3] = {nx, ny, nz};
   for (int d = 0; d < 3; ++d) {
     std::string why;
@@ -685,6 +762,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
                                              " does not fit one shared-memory tile at this precision");
     }
     e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
+    if (d > 0 && fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
     int rc = upload_twiddles(e->ax[d], prec);
     if (rc != GBFFT_OK) {
       release(e);
@@ -717,6 +795,11 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
     }
     cudaMemset(e->d_sync, 0, (size_t)(nz + 2) * sizeof(int));
   }
+  // tuned tile shapes and fusion for this shape, when the cache has them
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
+    if (tune.L[k] > 0 && gbfft_engine_set_tile(e, k, tune.L[k]) != GBFFT_OK) e->tile_L[k] = 0;
+  if (tune.fuse >= 0) e->fuse = tune.fuse != 0;
+  g_err.clear();
   *engine = e;
   return GBFFT_OK;
 }
@@ -868,7 +951,7 @@ int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
   const bool contig_pass = (kind == GBFFT_PASS_C2C_X) ||
                            ((kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R) &&
                             e->format == GBFFT_PHYSICAL_IN_X);
-  const int fe = fast_points(p.n, contig_pass);
+  const int fe = contig_pass ? fast_points(p.n, true) : p.fast_e;
   int tpl = fast ? p.n / fe : p.tpl;
   const int maxt = fast ? fast_max_threads(fe, e->prec) : kMaxThreads;
   if (!fast) {
@@ -908,6 +991,49 @@ int gbfft_selftest_bounded_wait(int counter_value, int need, long long poll_limi
   cudaFree(d);
   if (err != cudaSuccess) return cuda_fail(err, "bounded-wait self-test");
   *timed_out = h[1];
+  return GBFFT_OK;
+}
+
+int gbfft_tune_cache_path(const char* path) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_path_set = path != nullptr;
+  g_tune_path_override = path ? path : "";
+  g_tune_loaded = false;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_set_plan(gbfft_engine_t e, int axis, int points) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (axis < 1 || axis > 2) return fail(GBFFT_ERR_INVALID, "only the strided axes (1, 2) have plan choices");
+  AxisPlan& p = e->ax[axis];
+  if (!fast_has_alt(p.n)) return fail(GBFFT_ERR_UNSUPPORTED, "this axis length has one plan");
+  if (points != 16 && points != 32) return fail(GBFFT_ERR_INVALID, "points per thread must be 16 or 32");
+  if (p.fast_e == points) return GBFFT_OK;
+  void* old = p.d_twf;
+  const int old_e = p.fast_e;
+  p.fast_e = points;
+  p.d_twf = nullptr;
+  std::vector<int> radices;
+  for (int s = 0; s < fast_nst(p.n, points); ++s) radices.push_back(fast_radix(p.n, points, s));
+  int rc = upload_table(&p.d_twf, stage_twiddles(radices), e->prec);
+  if (rc != GBFFT_OK) {
+    p.fast_e = old_e;
+    p.d_twf = old;
+    return rc;
+  }
+  cudaDeviceSynchronize();  // no pass still reads the old table
+  if (old) cudaFree(old);
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k) e->tile_L[k] = 0;  // tiles were sized for the old plan
+  return GBFFT_OK;
+}
+
+int gbfft_engine_get_tuning(gbfft_engine_t e, int* fuse, int* tiles, int* points) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (fuse) *fuse = e->fuse ? 1 : 0;
+  if (tiles)
+    for (int k = 0; k < GBFFT_PASS_KINDS; ++k) tiles[k] = e->tile_L[k];
+  if (points)
+    for (int d = 0; d < 3; ++d) points[d] = fast_length(e->ax[d].n) ? e->ax[d].fast_e : 0;
   return GBFFT_OK;
 }
 

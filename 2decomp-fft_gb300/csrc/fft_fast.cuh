@@ -118,10 +118,9 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
 // at most 64 registers a thread, so a 512-thread strided tile still runs two
 // CTAs per SM.  32 points a thread: at most 256 threads and two CTAs per SM
 // (128 registers).
-template <typename T, int KIND, bool CONTIG, int N>
-__global__ void __launch_bounds__(fast_max_threads(fast_points(N, CONTIG), sizeof(T)), sizeof(T) == 4 ? 2 : 1)
+template <typename T, int KIND, bool CONTIG, int N, int E>
+__global__ void __launch_bounds__(fast_max_threads(E, sizeof(T)), sizeof(T) == 4 ? 2 : 1)
     fast_pass_kernel(const __grid_constant__ PassArgs a) {
-  constexpr int E = fast_points(N, CONTIG);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* Sm = reinterpret_cast<Cx<T>*>(smem_raw);
   LineCtx<T, KIND, CONTIG> c;
@@ -131,20 +130,32 @@ __global__ void __launch_bounds__(fast_max_threads(fast_points(N, CONTIG), sizeo
   if constexpr (KIND == K_R2C) c.store_r2c(Sm);
 }
 
-template <typename T, int KIND, bool CONTIG, int N>
-cudaError_t launch_n(const PassArgs& a, cudaStream_t stream) {
+template <typename T, int KIND, bool CONTIG, int N, int E>
+cudaError_t launch_ne(const PassArgs& a, cudaStream_t stream) {
   const size_t smem = (size_t)fast_smem_entries(N, a.L) * sizeof(Cx<T>);
-  auto kern = fast_pass_kernel<T, KIND, CONTIG, N>;
+  auto kern = fast_pass_kernel<T, KIND, CONTIG, N, E>;
   if (smem > 48 * 1024) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
   }
-  constexpr int TPL = N / fast_points(N, CONTIG);
+  constexpr int TPL = N / E;
   const dim3 block = CONTIG ? dim3(TPL, a.L) : dim3(a.L, TPL);
   const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
   kern<<<grid, block, smem, stream>>>(a);
   add_launches(1);
   return cudaGetLastError();
+}
+
+// Strided lines of 512 and 1024 points have two plans: 32 points a thread
+// (two stages, the default) or 16 (three stages); a.tpl says which.
+template <typename T, int KIND, bool CONTIG, int N>
+cudaError_t launch_n(const PassArgs& a, cudaStream_t stream) {
+  if constexpr (!CONTIG && (N == 512 || N == 1024)) {
+    if (a.tpl == N / 16) return launch_ne<T, KIND, CONTIG, N, 16>(a, stream);
+    return launch_ne<T, KIND, CONTIG, N, 32>(a, stream);
+  } else {
+    return launch_ne<T, KIND, CONTIG, N, fast_points(N, CONTIG)>(a, stream);
+  }
 }
 
 template <typename T, int KIND, bool CONTIG>

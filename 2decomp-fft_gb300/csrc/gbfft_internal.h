@@ -75,6 +75,8 @@ __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c
 __host__ __device__ constexpr int fast_points(int n, bool contiguous) {
   return (!contiguous && (n == 512 || n == 1024)) ? 32 : 16;
 }
+// Lengths whose strided passes also have the other plan (16 points a thread).
+__host__ __device__ constexpr bool fast_has_alt(int n) { return n == 512 || n == 1024; }
 __host__ __device__ constexpr int fast_nst(int n, int e) {
   return e == 32 ? 2 : ilog2c(n) / 4 + (ilog2c(n) % 4 ? 1 : 0);
 }

@@ -66,6 +66,9 @@ SIGNATURES = {
     "gbfft_engine_set_tile": (_i, [_vp, _i, _i]),
     "gbfft_engine_set_fusion": (_i, [_vp, _i]),
     "gbfft_engine_status": (_i, [_vp]),
+    "gbfft_tune_cache_path": (_i, [ctypes.c_char_p]),
+    "gbfft_engine_set_plan": (_i, [_vp, _i, _i]),
+    "gbfft_engine_get_tuning": (_i, [_vp, _ip, _ip, _ip]),
     "gbfft_engine_profile_read": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "gbfft_exec_c2r_noalloc": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp]),
@@ -222,6 +225,17 @@ class Engine:
         """Fuse the x and y passes of each z-plane into one kernel (default on)."""
         check(lib().gbfft_engine_set_fusion(self.h, int(bool(enable))))
 
+    def set_plan(self, axis, points):
+        """Strided axis 1/2 of 512 or 1024 points: 16 or 32 points per thread."""
+        check(lib().gbfft_engine_set_plan(self.h, int(axis), int(points)))
+
+    def tuning(self):
+        f = ctypes.c_int()
+        tiles = (ctypes.c_int * len(PASS_NAMES))()
+        pts = (ctypes.c_int * 3)()
+        check(lib().gbfft_engine_get_tuning(self.h, ctypes.byref(f), tiles, pts))
+        return {"fuse": bool(f.value), "tiles": dict(zip(PASS_NAMES, tiles)), "points": tuple(pts)}
+
     def status(self):
         """Raise GbfftError if the last fused pass gave up on a bounded wait."""
         check(lib().gbfft_engine_status(self.h))
@@ -257,6 +271,12 @@ class Engine:
 
 
 NOALLOC_SCRATCH_BYTES = 64 * 1024 * 1024
+
+
+def set_tune_cache(path):
+    """Tuning cache for engines created from now on: a path, "" for none,
+    None for the default (tune_cache.txt in the package directory)."""
+    check(lib().gbfft_tune_cache_path(None if path is None else path.encode()))
 
 
 def c2r_noalloc(fmt, nx, ny, nz, prec, x, out, stream=None):

@@ -1,0 +1,151 @@
+"""Autotuner of the GB300 FFT backend.
+
+For each grid shape it measures, on the GPU at hand, the choices an engine
+can make and writes the fastest into the tuning cache that engines read at
+creation (tune_cache.txt beside this file, or $GBFFT_TUNE_CACHE):
+
+  * the radix plan of strided axes of 512 or 1024 points: 16 points per
+    thread (radix 16 stages) or 32 (two radix-32 stages)      -> e_y, e_z
+  * the tile shape (lines per CTA) of every pass kind          -> r2c, c2r,
+                                                                  c2c_x, c2c_y,
+                                                                  c2c_z, xy_fused
+  * pass fusion: x and y passes of each z-plane in one kernel  -> fuse
+
+The measured step is the benchmark's: one r2c then one c2r, per-pass device
+times from CUDA events on the launching stream.
+
+    python tune.py [--out FILE] [--shapes prec,fmt,nx,ny,nz ...]
+"""
+import argparse
+import itertools
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+import gbfft  # noqa: E402
+
+# prec format nx ny nz: the benchmark's grids
+DEFAULT_SHAPES = [
+    (4, 1, 1024, 1024, 512), (4, 3, 1024, 1024, 512),
+    (4, 1, 384, 400, 243), (8, 1, 384, 400, 243),
+    (4, 1, 360, 270, 210), (8, 1, 360, 270, 210),
+    (4, 1, 256, 256, 256), (8, 1, 64, 64, 64),
+]
+TILES = [1, 2, 4, 8, 16, 32]
+
+
+def measure(eng, x, s, y, steps=6, warm=2):
+    """{pass: ms per launch} and the step time in ms."""
+    import torch
+    for _ in range(warm):
+        eng.r2c(x, s)
+        eng.c2r(s, y)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        eng.r2c(x, s)
+        eng.c2r(s, y)
+    e1.record()
+    torch.cuda.synchronize()
+    step = e0.elapsed_time(e1) / steps
+    eng.set_profiling(True)
+    for _ in range(steps):
+        eng.r2c(x, s)
+        eng.c2r(s, y)
+    torch.cuda.synchronize()
+    prof = eng.profile()
+    eng.set_profiling(False)
+    return {k: v[1] / v[0] for k, v in prof.items()}, step
+
+
+def tune_shape(prec, fmt, nx, ny, nz, log=print):
+    import torch
+    rdt = torch.float32 if prec == 4 else torch.float64
+    eng = gbfft.Engine(fmt, nx, ny, nz, prec=prec)
+    x = torch.randn((nz, ny, nx), dtype=rdt, device="cuda")
+    s = eng.empty_spectral()
+    y = eng.empty_physical()
+    opts = {}
+    for axis, n in ((1, ny), (2, nz)):
+        opts[axis] = [16, 32] if n in (512, 1024) else [None]
+    eng.set_fusion(False)
+    best = None
+    for ey, ez in itertools.product(opts[1], opts[2]):
+        if ey:
+            eng.set_plan(1, ey)
+        if ez:
+            eng.set_plan(2, ez)
+        times, _ = measure(eng, x, s, y)
+        tiles = {}
+        total = 0.0
+        for kind, t0 in times.items():
+            bt, bl = t0, 0
+            for L in TILES:
+                try:
+                    eng.set_tile(kind, L)
+                except gbfft.GbfftError:
+                    continue
+                t = measure(eng, x, s, y, steps=4, warm=1)[0].get(kind, t0)
+                if t < bt:
+                    bt, bl = t, L
+                eng.set_tile(kind, 0)
+            tiles[kind] = bl
+            mult = 2 if kind.startswith("c2c") else 1
+            total += mult * bt
+        log("  plan e_y=%s e_z=%s: est %.4f ms %s" % (ey, ez, total, tiles))
+        if best is None or total < best[0]:
+            best = (total, ey, ez, tiles)
+    total, ey, ez, tiles = best
+    if ey:
+        eng.set_plan(1, ey)
+    if ez:
+        eng.set_plan(2, ez)
+    for kind, L in tiles.items():
+        if L:
+            eng.set_tile(kind, L)
+    _, step_plain = measure(eng, x, s, y)
+    fuse = 0
+    eng.set_fusion(True)
+    times_f, step_fused = measure(eng, x, s, y)
+    if "xy_fused" in times_f and step_fused < step_plain:
+        fuse = 1
+    log("  step %.4f ms unfused, %.4f ms fused%s" % (step_plain, step_fused,
+                                                    "" if "xy_fused" in times_f else " (no fused kernel)"))
+    eng.close()
+    fields = ["%d %d %d %d %d" % (prec, fmt, nx, ny, nz), "fuse=%d" % fuse]
+    if ey:
+        fields.append("e_y=%d" % ey)
+    if ez:
+        fields.append("e_z=%d" % ez)
+    for kind, L in sorted(tiles.items()):
+        if L:
+            fields.append("%s=%d" % (kind, L))
+    return " ".join(fields), min(step_plain, step_fused if fuse else step_plain)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=os.path.join(HERE, "tune_cache.txt"))
+    ap.add_argument("--shapes", nargs="*", help="prec,fmt,nx,ny,nz")
+    args = ap.parse_args()
+    shapes = [tuple(int(v) for v in s.split(",")) for s in args.shapes] if args.shapes else DEFAULT_SHAPES
+    gbfft.lib()
+    gbfft.set_tune_cache("")  # measure from the built-in choices
+    lines = ["# GB300 tuning cache written by tune.py: prec format nx ny nz key=value ...",
+             "# keys: fuse, e_y/e_z (points per thread of strided plans), lines per CTA per pass"]
+    for shp in shapes:
+        print("shape", shp, flush=True)
+        line, ms = tune_shape(*shp)
+        print("  ->", line, "(%.4f ms)" % ms, flush=True)
+        lines.append(line)
+    with open(args.out, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    print("wrote", args.out)
+
+
+if __name__ == "__main__":
+    main()

@@ -180,6 +180,23 @@ int gbfft_engine_set_tile(gbfft_engine_t engine, int kind, int lines_per_cta);
  * one kernel per axis. */
 int gbfft_engine_set_fusion(gbfft_engine_t engine, int enable);
 
+/* ---- autotuning ---------------------------------------------------------
+ * Engines apply a tuning cache at creation: a text file (default
+ * tune_cache.txt in the package directory, or $GBFFT_TUNE_CACHE; "" = none)
+ * with lines "prec format nx ny nz key=value ...": per pass kind the lines
+ * per CTA (r2c c2r c2c_x c2c_y c2c_z xy_fused), fuse=0/1, and e_y / e_z,
+ * the points per thread of the strided y / z plan (16: radix 16, 16, ...;
+ * 32: two radix-32 stages) for axes of 512 or 1024 points.  The tuner
+ * (2decomp-fft_gb300/tune.py) measures the choices and writes the file. */
+int gbfft_tune_cache_path(const char* path); /* NULL = default, "" = none */
+/* Re-plan strided axis 1 or 2 (512 or 1024 points) with 16 or 32 points per
+ * thread; resets the tile shapes.  Waits for the device. */
+int gbfft_engine_set_plan(gbfft_engine_t engine, int axis, int points);
+/* Current fusion switch, lines per CTA per pass kind (GBFFT_PASS_KINDS
+ * ints, 0 = built-in) and points per thread per axis (3 ints, 0 = the axis
+ * has no compile-time plan). */
+int gbfft_engine_get_tuning(gbfft_engine_t engine, int* fuse, int* tiles, int* points);
+
 /* Status of the engine's most recent fused x/y pass: waits for the device,
  * returns GBFFT_ERR_TIMEOUT if one of its bounded inter-CTA waits gave up
  * (the result of that transform is then invalid), GBFFT_OK otherwise.  The

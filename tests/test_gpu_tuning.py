@@ -1,0 +1,76 @@
+"""GPU: the tuning knobs change speed, never results.
+
+Every choice the autotuner can make -- strided plan (16 or 32 points per
+thread), tile shape per pass, pass fusion -- must give the same spectrum
+(within the FP32 tolerance against the FP64 oracle), and a cache line must be
+applied to the engines created after it is read."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("fmt", [1, 3])
+@pytest.mark.parametrize("ey,ez", [(16, 16), (32, 16), (16, 32), (32, 32)])
+def test_strided_plans_give_the_same_transform(fmt, ey, ez):
+    import gbfft
+    nx, ny, nz = 64, 1024, 512
+    x = np.random.default_rng(ey + ez + fmt).standard_normal((nz, ny, nx))
+    e = gbfft.Engine(fmt, nx, ny, nz, prec=gbfft.PREC_SINGLE)
+    e.set_plan(1, ey)
+    e.set_plan(2, ez)
+    assert e.tuning()["points"][1:] == (ey, ez)
+    xd = torch.from_numpy(x.astype(np.float32)).cuda()
+    s = e.empty_spectral()
+    e.r2c(xd, s)
+    assert rel(s.cpu().numpy(), O.fft3d_r2c(x, fmt)) <= 2e-6
+    y = e.empty_physical()
+    e.c2r(s, y)
+    assert rel(y.cpu().numpy() / (nx * ny * nz), x) <= 2e-6
+    e.close()
+
+
+def test_tile_shapes_give_the_same_transform():
+    import gbfft
+    nx, ny, nz = 256, 64, 48
+    x = np.random.default_rng(3).standard_normal((nz, ny, nx))
+    ref = O.fft3d_r2c(x, 1)
+    e = gbfft.Engine(1, nx, ny, nz, prec=gbfft.PREC_SINGLE)
+    xd = torch.from_numpy(x.astype(np.float32)).cuda()
+    s = e.empty_spectral()
+    for kind in ("r2c", "c2c_y", "c2c_z"):
+        for L in (1, 2, 4, 8, 16):
+            try:
+                e.set_tile(kind, L)
+            except gbfft.GbfftError:
+                continue
+            e.r2c(xd, s)
+            assert rel(s.cpu().numpy(), ref) <= 2e-6, (kind, L)
+        e.set_tile(kind, 0)
+    e.close()
+
+
+def test_cache_line_is_applied(tmp_path):
+    import gbfft
+    path = tmp_path / "cache.txt"
+    path.write_text("# test\n4 1 64 1024 512 fuse=0 e_y=16 e_z=32 c2c_y=4 r2c=2\n")
+    gbfft.set_tune_cache(str(path))
+    try:
+        e = gbfft.Engine(1, 64, 1024, 512, prec=gbfft.PREC_SINGLE)
+        t = e.tuning()
+        assert t["points"][1:] == (16, 32)
+        assert t["tiles"]["c2c_y"] == 4 and t["tiles"]["r2c"] == 2
+        assert t["fuse"] is False
+        e.close()
+        other = gbfft.Engine(1, 64, 1024, 256, prec=gbfft.PREC_SINGLE)
+        assert other.tuning()["tiles"]["c2c_y"] == 0  # no line for this shape
+        other.close()
+    finally:
+        gbfft.set_tune_cache(None)
