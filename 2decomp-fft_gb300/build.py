@@ -35,7 +35,7 @@ def sources():
 
 
 def _newest_input():
-    files = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    files = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)

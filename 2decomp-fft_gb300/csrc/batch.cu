@@ -106,7 +106,7 @@ int build_desc(gbfft_batch_t b, int mask) {
       per[g].insert(per[g].end(), buf, buf + n);
     }
     for (const PassInfo& p : per[g])
-      if (!p.a.fast || !batch_length(p.a.n)) {
+      if ((p.a.fast != 1 && p.a.fast != 2) || !batch_length(p.a.n)) {
         b->built_mask = mask;
         return GBFFT_OK;
       }

@@ -393,7 +393,21 @@ int mixed_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int 
   return L;
 }
 
-void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind, int forced_L) {
+void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind, int forced_L,
+               bool split = false) {
+  if (split && split_length(p.n)) {
+    a.n = p.n;
+    a.nst = 0;
+    a.tw = p.d_twf;
+    a.fast = 3;
+    a.L = split_lines_per_cta(p.n, contiguous);
+    a.tpl = 256 / a.L;
+    a.first_fused = 0;
+    a.last_fused = 0;
+    (void)forced_L;
+    (void)kind;
+    return;
+  }
   if (mixed_length(p.n)) {
     a.n = p.n;
     a.nst = 0;
@@ -469,7 +483,8 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
     a.nlines = n1;
     a.nv = n2;
   }
-  fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C, e->tile_L[GBFFT_PASS_C2C_X + axis]);
+  fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C, e->tile_L[GBFFT_PASS_C2C_X + axis],
+            e->form == GBFFT_FORM_SPLIT);
   P.prof_kind = GBFFT_PASS_C2C_X + axis;
   P.bytes = 2.0 * (double)n1 * n2 * n3 * (double)cbytes(e);
   return P;
@@ -519,7 +534,7 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst) {
   a.pair_vec = (!P.contiguous && nx % 2 == 0 && ((uintptr_t)real_ptr % (2 * (size_t)e->prec)) == 0) ? 1 : 0;
   const int axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, kind,
-            e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R]);
+            e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R], e->form == GBFFT_FORM_SPLIT);
   P.prof_kind = kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R;
   P.bytes = (double)nx * ny * nz * e->prec +
             (double)e->sp[0] * e->sp[1] * e->sp[2] * (double)cbytes(e);
@@ -530,7 +545,7 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst) {
 // by one fused x/y kernel when one exists for the lengths.  `planes` is the
 // z extent of the array the two passes work on.
 void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
-  if (!e->d_sync || planes > e->sync_planes) return;
+  if (!e->d_sync || planes > e->sync_planes || e->form == GBFFT_FORM_SPLIT) return;
   for (size_t i = 0; i + 1 < ps.size(); ++i) {
     Pass& p0 = ps[i];
     Pass& p1 = ps[i + 1];
@@ -724,8 +739,8 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
     return fail(GBFFT_ERR_INVALID, "Invalid value for precision (4 or 8)");
   if (form != GBFFT_FORM_PLAIN && form != GBFFT_FORM_SPLIT)
     return fail(GBFFT_ERR_INVALID, "Invalid value for form");
-  if (form == GBFFT_FORM_SPLIT)
-    return fail(GBFFT_ERR_UNSUPPORTED, "split tensor-core form is not available in this build");
+  if (form == GBFFT_FORM_SPLIT && prec != GBFFT_PREC_SINGLE)
+    return fail(GBFFT_ERR_UNSUPPORTED, "the split tensor-core form works on single-precision data");
   const long long cells = (long long)nx * ny * nz;
   if (cells > (1LL << 40)) return fail(GBFFT_ERR_UNSUPPORTED, "grid too large");
   if ((long long)ny * nz > 0x7fffffffLL || (long long)nx * ny > 0x7fffffffLL)
@@ -763,6 +778,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
     }
     e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
     if (d > 0 && fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
+    if (form == GBFFT_FORM_SPLIT) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
     int rc = upload_twiddles(e->ax[d], prec);
     if (rc != GBFFT_OK) {
       release(e);
@@ -1006,6 +1022,7 @@ int gbfft_engine_set_plan(gbfft_engine_t e, int axis, int points) {
   if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
   if (axis < 1 || axis > 2) return fail(GBFFT_ERR_INVALID, "only the strided axes (1, 2) have plan choices");
   AxisPlan& p = e->ax[axis];
+  if (e->form == GBFFT_FORM_SPLIT) return fail(GBFFT_ERR_UNSUPPORTED, "the split form has one plan");
   if (!fast_has_alt(p.n)) return fail(GBFFT_ERR_UNSUPPORTED, "this axis length has one plan");
   if (points != 16 && points != 32) return fail(GBFFT_ERR_INVALID, "points per thread must be 16 or 32");
   if (p.fast_e == points) return GBFFT_OK;

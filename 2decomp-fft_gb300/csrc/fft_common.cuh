@@ -260,6 +260,11 @@ struct LineCtx {
     const int a = CONTIG ? line * N + n : n * L + line;
     return a + (a >> 4);
   }
+  // slot of point n of any line of the tile (same layout as sidx)
+  __device__ __forceinline__ int sidx_at(int line_, int n) const {
+    const int a = CONTIG ? line_ * N + n : n * L + line_;
+    return a + (a >> 4);
+  }
   __device__ __forceinline__ C twiddle(int e) const { return __ldg(tw + e); }
 
   // Point n of the complex line this thread works on, as the forward

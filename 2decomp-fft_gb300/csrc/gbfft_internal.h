@@ -56,7 +56,8 @@ struct PassArgs {
   int nv;          // strided: extent of v (grid.y)
   int first_fused; // stage 0 reads global memory directly
   int last_fused;  // last stage writes global memory directly
-  int fast;        // 1: compile-time power-of-two kernel, 2: mixed-radix kernel
+  int fast;        // 1: compile-time power-of-two kernel, 2: mixed-radix kernel,
+                   // 3: split-precision tensor-core kernel
   int pair_vec;    // r2c/c2r on strided lines: the two real lines of a pair
                    // are adjacent and 8-byte aligned (read/write as one pair)
   int radix[kMaxStages];
@@ -98,6 +99,11 @@ __host__ __device__ constexpr bool mixed_length(int n) {
          n == 384 || n == 400;
 }
 cudaError_t launch_mixed_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+// Split-precision tensor-core passes (fft_split.cuh): FP32 lines of 256,
+// 512, 1024 points, 256-thread CTAs of split_lines_per_cta lines.
+bool split_length(int n);
+int split_lines_per_cta(int n, bool contiguous);
+cudaError_t launch_split_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 cudaError_t launch_mixed_f64(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 
 // Thread limit of the power-of-two kernel for E points a thread.

@@ -289,7 +289,8 @@ def run_gb300(args):
     rdt = torch.float32 if prec == 4 else torch.float64
     gbfft.lib()
 
-    eng = gbfft.Engine(fmt, nx, ny, nz, prec=prec)
+    form = gbfft.FORM_SPLIT if args.form == "split" else gbfft.FORM_PLAIN
+    eng = gbfft.Engine(fmt, nx, ny, nz, prec=prec, form=form)
     x = make_input(nx, ny, nz, kind, rdt, dev)
     spec = eng.empty_spectral(device=dev)
     y = torch.empty_like(x)
@@ -369,7 +370,8 @@ def run_gb300(args):
         d = passes[dom]
         roof = {"bound": "hbm", "kernel": "axis pass %s" % dom, "achieved": round(d["gbs"], 1),
                 "peak": peak, "unit": "GB/s", "frac": round(d["gbs"] / peak, 4),
-                "traffic": read_traffic(args.workload, dom), "peak_source": peak_src,
+                "traffic": read_traffic(args.workload + ("" if args.form == "plain" else ":" + args.form), dom),
+                "peak_source": peak_src,
                 "step_frac": round(algo_bytes_step / (ms_max * 1e-3) / 1e9 / peak, 4)}
 
     # end to end through the C ABI with host buffers
@@ -433,7 +435,7 @@ def run_gb300(args):
                                        else "seeded uniform [-1,1)"),
             "config": {"workload": "r2c+c2r round trip %dx%dx%d %s %s" % (
                 nx, ny, nz, "fp32" if prec == 4 else "fp64", "PHYSICAL_IN_X" if fmt == 1 else "PHYSICAL_IN_Z"),
-                "name": args.workload, "nx": nx, "ny": ny, "nz": nz, "form": "plain",
+                "name": args.workload, "nx": nx, "ny": ny, "nz": nz, "form": args.form,
                 "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas (one grid per GPU)"},
             "roofline": roof,
             "passes": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
@@ -628,6 +630,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [BATCH_WORKLOAD])
+    ap.add_argument("--form", default="plain", choices=["plain", "split"],
+                    help="plain FP32/FP64 stages, or split-FP16 tensor-core radix-16 stages (FP32 only)")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

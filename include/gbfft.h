@@ -46,7 +46,9 @@ extern "C" {
 
 /* arithmetic form of the axis passes */
 #define GBFFT_FORM_PLAIN 0 /* CUDA-core FP32 / FP64 butterflies              */
-#define GBFFT_FORM_SPLIT 1 /* radix-16 stages as split-FP16 tensor-core DFTs  */
+#define GBFFT_FORM_SPLIT 1 /* radix-16 stages as split-FP16 tensor-core DFTs
+                              (FP32 data; axes of 256, 512, 1024 points; other
+                              axes run the plain kernels) */
 
 /* transpose kinds (src/decomp_2d.f90:140-222 generic transpose_* names) */
 #define GBFFT_X_TO_Y 0
