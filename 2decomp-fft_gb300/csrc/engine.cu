@@ -191,6 +191,9 @@ struct TuneEntry {
   int prec = 0, format = 0, nx = 0, ny = 0, nz = 0;
   int fuse = -1;
   int L[GBFFT_PASS_KINDS] = {0};
+  int pipe[GBFFT_PASS_KINDS] = {0};
+  int csize[GBFFT_PASS_KINDS] = {0};
+  int csync[GBFFT_PASS_KINDS] = {0};
   int e[3] = {0, 0, 0};
 };
 
@@ -237,8 +240,12 @@ void load_tune_locked() {
       if (k == "fuse") t.fuse = v;
       else if (k == "e_y") t.e[1] = v;
       else if (k == "e_z") t.e[2] = v;
-      for (int i = 0; i < GBFFT_PASS_KINDS; ++i)
+      for (int i = 0; i < GBFFT_PASS_KINDS; ++i) {
         if (k == names[i]) t.L[i] = v;
+        if (k == std::string("pipe_") + names[i]) t.pipe[i] = v;
+        if (k == std::string("cl_") + names[i]) t.csize[i] = v;
+        if (k == std::string("cls_") + names[i]) t.csync[i] = v;
+      }
     }
     g_tune.push_back(t);
   }
@@ -277,6 +284,9 @@ struct gbfft_engine_s {
   int sp[3] = {0, 0, 0};
   AxisPlan ax[3];
   int tile_L[GBFFT_PASS_KINDS] = {0};  // tuned lines per CTA, 0 = built-in
+  int pipe[GBFFT_PASS_KINDS] = {0};    // tile buffers of the pipelined kernel, 0 = one-shot
+  int csize[GBFFT_PASS_KINDS] = {0};   // cluster launch of the one-shot kernel, 0 = none
+  int csync[GBFFT_PASS_KINDS] = {0};   // with it, a cluster barrier at the start
   bool fuse = false;                   // fuse x/y passes per plane when possible
   int* d_sync = nullptr;               // fused kernel's ticket/status/plane counters
   long long sync_planes = 0;
@@ -394,7 +404,7 @@ int mixed_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int 
 }
 
 void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind, int forced_L,
-               bool split = false) {
+               bool split = false, int pipe = 0, int csize = 0, int csync = 0) {
   if (split && split_length(p.n)) {
     a.n = p.n;
     a.nst = 0;
@@ -429,7 +439,27 @@ void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int ki
     a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L, fe);
     a.first_fused = 1;
     a.last_fused = kind != K_R2C;
-    (void)kind;
+    a.pipe = 0;
+    a.csize = csize > 1 ? csize : 0;
+    a.csync = a.csize ? csync : 0;
+    if (pipe > 0 && prec == 4 && pipe_length(p.n)) {
+      // power-of-two tile heights only (the copy loop indexes by shifts),
+      // and every buffer of the CTA within the shared-memory limit
+      int L = 1;
+      while (2 * L <= a.L) L *= 2;
+      if (contiguous && forced_L <= 0) {
+        L = 1;
+        while (2 * L * a.tpl <= 256) L *= 2;
+      }
+      while (L > 1 && L * a.tpl > pipe_max_threads(fe)) L /= 2;
+      while (L > 1 && (size_t)pipe * fast_smem_entries(p.n, L) * sizeof(float2) > kPipeSmemLimit) L /= 2;
+      if ((size_t)pipe * fast_smem_entries(p.n, L) * sizeof(float2) <= kPipeSmemLimit) {
+        a.L = L;
+        a.pipe = pipe;
+        a.csize = 0;
+        a.csync = 0;
+      }
+    }
     return;
   }
   a.n = p.n;
@@ -484,7 +514,8 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
     a.nv = n2;
   }
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C, e->tile_L[GBFFT_PASS_C2C_X + axis],
-            e->form == GBFFT_FORM_SPLIT);
+            e->form == GBFFT_FORM_SPLIT, e->pipe[GBFFT_PASS_C2C_X + axis], e->csize[GBFFT_PASS_C2C_X + axis],
+            e->csync[GBFFT_PASS_C2C_X + axis]);
   P.prof_kind = GBFFT_PASS_C2C_X + axis;
   P.bytes = 2.0 * (double)n1 * n2 * n3 * (double)cbytes(e);
   return P;
@@ -534,7 +565,10 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst) {
   a.pair_vec = (!P.contiguous && nx % 2 == 0 && ((uintptr_t)real_ptr % (2 * (size_t)e->prec)) == 0) ? 1 : 0;
   const int axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, kind,
-            e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R], e->form == GBFFT_FORM_SPLIT);
+            e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R], e->form == GBFFT_FORM_SPLIT,
+            e->pipe[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R],
+            e->csize[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R],
+            e->csync[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R]);
   P.prof_kind = kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R;
   P.bytes = (double)nx * ny * nz * e->prec +
             (double)e->sp[0] * e->sp[1] * e->sp[2] * (double)cbytes(e);
@@ -560,6 +594,7 @@ void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
     Pass& py = xfirst ? p1 : p0;
     if (p1.a.src != p0.a.dst) continue;
     if (!fast_length(px.a.n) || !fast_length(py.a.n)) continue;
+    if (px.a.fast != 1 || py.a.fast != 1 || px.a.pipe || py.a.pipe || px.a.csize || py.a.csize) continue;
     if (e->ax[1].fast_e != fast_points(py.a.n, false)) continue;  // the fused kernel's y plan
     if (!fused_supported(e->prec, px.kind, xfirst, px.a.n, py.a.n)) continue;
     long long per_plane;
@@ -574,13 +609,17 @@ void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
     F.fused = true;
     F.fused_kindx = px.kind;
     F.fused_xfirst = xfirst;
+    // tile shape: tile_L[XY] y lines a tile (threads = lines x y threads a line)
+    const int ty = py.a.n / fast_points(py.a.n, false);
+    const int th = e->tile_L[GBFFT_PASS_XY] ? e->tile_L[GBFFT_PASS_XY] * ty : kFusedThreads;
+    F.f.threads = th;
     F.f.ax = px.a;
     F.f.ax.nlines = (int)per_plane;
     F.f.ax.tpl = px.a.n / fast_points(px.a.n, true);
-    F.f.ax.L = kFusedThreads / F.f.ax.tpl;
+    F.f.ax.L = th / F.f.ax.tpl;
     F.f.ay = py.a;
-    F.f.ay.tpl = py.a.n / fast_points(py.a.n, false);
-    F.f.ay.L = kFusedThreads / F.f.ay.tpl;
+    F.f.ay.tpl = ty;
+    F.f.ay.L = th / ty;
     F.f.nplanes = planes;
     F.f.sync = e->d_sync;
     F.prof_kind = GBFFT_PASS_XY;
@@ -814,6 +853,13 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
   // tuned tile shapes and fusion for this shape, when the cache has them
   for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
     if (tune.L[k] > 0 && gbfft_engine_set_tile(e, k, tune.L[k]) != GBFFT_OK) e->tile_L[k] = 0;
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
+    if (tune.pipe[k] > 0 && gbfft_engine_set_pipeline(e, k, tune.pipe[k]) != GBFFT_OK) e->pipe[k] = 0;
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
+    if (tune.csize[k] > 0 && gbfft_engine_set_cluster(e, k, tune.csize[k], tune.csync[k]) != GBFFT_OK) {
+      e->csize[k] = 0;
+      e->csync[k] = 0;
+    }
   if (tune.fuse >= 0) e->fuse = tune.fuse != 0;
   g_err.clear();
   *engine = e;
@@ -949,6 +995,14 @@ int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
     e->tile_L[kind] = 0;
     return GBFFT_OK;
   }
+  if (kind == GBFFT_PASS_XY) {
+    // fused x/y kernel: y lines a tile, 256 or 512 threads a CTA
+    const int ty = fast_length(e->ny) ? e->ny / fast_points(e->ny, false) : 0;
+    if (ty == 0 || (lines * ty != 256 && lines * ty != 512))
+      return fail(GBFFT_ERR_INVALID, "fused tiles have 256 or 512 threads");
+    e->tile_L[kind] = lines;
+    return GBFFT_OK;
+  }
   int axis;
   if (kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R)
     axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
@@ -982,6 +1036,39 @@ int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
                             : pass_smem_bytes(e->prec, p.n, lines);
   if (smem > 200 * 1024) return fail(GBFFT_ERR_INVALID, "tile exceeds the shared-memory limit");
   e->tile_L[kind] = lines;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_set_pipeline(gbfft_engine_t e, int kind, int depth) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (kind < 0 || kind >= GBFFT_PASS_KINDS) return fail(GBFFT_ERR_INVALID, "bad pass kind");
+  if (depth != 0 && depth != 2 && depth != 3) return fail(GBFFT_ERR_INVALID, "pipeline depth must be 0, 2 or 3");
+  e->pipe[kind] = depth;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_set_cluster(gbfft_engine_t e, int kind, int ctas, int sync) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  if (kind < 0 || kind >= GBFFT_PASS_KINDS) return fail(GBFFT_ERR_INVALID, "bad pass kind");
+  if (ctas != 0 && ctas != 2 && ctas != 4 && ctas != 8)
+    return fail(GBFFT_ERR_INVALID, "cluster size must be 0, 2, 4 or 8");
+  e->csize[kind] = ctas;
+  e->csync[kind] = ctas ? (sync != 0) : 0;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_get_cluster(gbfft_engine_t e, int* ctas, int* sync) {
+  if (!valid_engine(e) || !ctas || !sync) return fail(GBFFT_ERR_INVALID, "bad argument");
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k) {
+    ctas[k] = e->csize[k];
+    sync[k] = e->csync[k];
+  }
+  return GBFFT_OK;
+}
+
+int gbfft_engine_get_pipeline(gbfft_engine_t e, int* depth) {
+  if (!valid_engine(e) || !depth) return fail(GBFFT_ERR_INVALID, "bad argument");
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k) depth[k] = e->pipe[k];
   return GBFFT_OK;
 }
 

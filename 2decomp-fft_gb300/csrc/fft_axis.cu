@@ -198,6 +198,10 @@ size_t pass_smem_bytes(int prec_bytes, int n, int L) {
 
 cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a,
                              cudaStream_t stream) {
+  if (a.fast == 1 && a.pipe) {
+    if (prec_bytes != 4) return cudaErrorInvalidValue;
+    return launch_pipe_f32(kind, contiguous, a, stream);
+  }
   if (a.fast == 3) {
     if (prec_bytes != 4) return cudaErrorInvalidValue;
     return launch_split_f32(kind, contiguous, a, stream);

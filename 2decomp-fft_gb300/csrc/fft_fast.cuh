@@ -20,6 +20,8 @@
 //    the thread index, so no integer division is left in the loop body.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "fft_common.cuh"
 
 namespace gbfft {
@@ -47,7 +49,10 @@ template <bool WARP_LOCAL> __device__ __forceinline__ void stage_barrier() {
   else __syncthreads();
 }
 
-template <int N, int E, int S, class Ctx, class C>
+// SMEM0: stage 0 reads its points from Sm (already filled by the caller:
+// natural order for c2c / r2c, the staged half spectra for c2r) instead of
+// global memory.
+template <int N, int E, int S, class Ctx, class C, bool SMEM0 = false>
 __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
   using P = P2Plan<N, E>;
   constexpr int KIND = Ctx::kind;
@@ -59,12 +64,22 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
     if constexpr (FIRST && KIND == K_C2R) {
       // half spectra staged in shared memory (each value read from global
       // memory once, coalesced), then the Hermitian gather
-      c.template stage_c2r<N, TPL>(Sm);
-      __syncthreads();
+      if constexpr (!SMEM0) {
+        c.template stage_c2r<N, TPL>(Sm);
+        __syncthreads();
+      }
 #pragma unroll
       for (int m = 0; m < MB; ++m)
 #pragma unroll
         for (int r = 0; r < R; ++r) v[m * R + r] = c.sgather_c2r(Sm, t + m * TPL + r * NB);
+      __syncthreads();
+    } else if constexpr (FIRST && SMEM0) {
+#pragma unroll
+      for (int m = 0; m < MB; ++m)
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[m * R + r] = c.sload(Sm, t + m * TPL + r * NB);
+      // all points of the tile are in registers before stage 0's outputs
+      // overwrite the buffer
       __syncthreads();
     } else if constexpr (FIRST) {
 #pragma unroll
@@ -98,6 +113,7 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
       }
     } else {
       if constexpr (!FIRST) stage_barrier<WL>();
+      // (SMEM0: the first stage synchronised after its shared-memory reads)
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         const int b = t + m * TPL;
@@ -110,19 +126,23 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
       if constexpr (LAST) __syncthreads();
       else stage_barrier<WL>();
     }
-    run_stages<N, E, S + 1>(c, Sm, v);
+    run_stages<N, E, S + 1, Ctx, C, SMEM0>(c, Sm, v);
   }
 }
 
-// 16 points a thread, FP32: at most 512 threads and two CTAs per SM, i.e.
-// at most 64 registers a thread, so a 512-thread strided tile still runs two
-// CTAs per SM.  32 points a thread: at most 256 threads and two CTAs per SM
-// (128 registers).
+// 16 points a thread, FP32: up to 1024 threads, i.e. at most 64 registers a
+// thread, so a 512-thread strided tile still runs two CTAs per SM and a
+// 1024-thread one (16 lines of 1024 points, 32 of 512: 128- and 256-byte
+// row segments on strided axes) one.  32 points a thread: up to 512
+// threads, at most 128 registers.
 template <typename T, int KIND, bool CONTIG, int N, int E>
-__global__ void __launch_bounds__(fast_max_threads(E, sizeof(T)), sizeof(T) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(fast_max_threads(E, sizeof(T)), 1)
     fast_pass_kernel(const __grid_constant__ PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* Sm = reinterpret_cast<Cx<T>*>(smem_raw);
+  // launched in clusters: start together, so that neighbouring CTAs' loads
+  // of the same rows are in the DRAM queues at the same time
+  if (a.csync) cooperative_groups::this_cluster().sync();
   LineCtx<T, KIND, CONTIG> c;
   c.init(a);
   Cx<T> v[E];
@@ -140,7 +160,27 @@ cudaError_t launch_ne(const PassArgs& a, cudaStream_t stream) {
   }
   constexpr int TPL = N / E;
   const dim3 block = CONTIG ? dim3(TPL, a.L) : dim3(a.L, TPL);
-  const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
+  const long long tiles = (a.nlines + a.L - 1) / a.L;
+  if (a.csize > 1) {
+    // grid.x padded to whole clusters; the padding CTAs own no line
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((tiles + a.csize - 1) / a.csize * a.csize), CONTIG ? 1u : (unsigned)a.nv, 1);
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)a.csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t err = cudaLaunchKernelEx(&cfg, kern, a);
+    add_launches(1);
+    return err != cudaSuccess ? err : cudaGetLastError();
+  }
+  if (a.csync) return cudaErrorInvalidValue;  // a cluster barrier needs a cluster launch
+  const dim3 grid((unsigned)tiles, CONTIG ? 1u : (unsigned)a.nv);
   kern<<<grid, block, smem, stream>>>(a);
   add_launches(1);
   return cudaGetLastError();

@@ -6,8 +6,8 @@
 // At one rank the reference runs the x and y transforms as two complete
 // passes over the array (src/fft_common_3d.f90:27-58 and :133-159, with
 // transposes that are copies in between).  Here the work of both passes is
-// cut into tiles (L lines of one axis within one plane, one 512-thread CTA
-// tile each) and dealt out through a ticket counter in a fixed order:
+// cut into tiles (L lines of one axis within one plane, one CTA of TH = 256
+// or 512 threads a tile) and dealt out through a ticket counter in a fixed order:
 //
 //   slot k:  phase-1 tiles of plane k,  then phase-2 tiles of plane k - LAG
 //
@@ -36,13 +36,12 @@ namespace fused {
 using namespace dev;
 using fast::run_stages;
 
-constexpr int kThreads = 512;
 constexpr int kLag = 2;
 constexpr long long kSpinLimit = 1ll << 24;  // ~1-2 s of polling
 
-template <typename T, int KIND, bool CG, int N>
+template <typename T, int KIND, bool CG, int N, int TH>
 __device__ __forceinline__ void x_tile(const PassArgs& a, Cx<T>* Sm, long long plane, int item) {
-  constexpr int EX = fast_points(N, true), TX = N / EX, LX = kThreads / TX;
+  constexpr int EX = fast_points(N, true), TX = N / EX, LX = TH / TX;
   const int tid = threadIdx.x;
   const int t = tid % TX, line = tid / TX;
   const long long per_plane = a.nlines;  // complex x lines in one plane
@@ -54,9 +53,9 @@ __device__ __forceinline__ void x_tile(const PassArgs& a, Cx<T>* Sm, long long p
   if constexpr (KIND == K_R2C) c.store_r2c(Sm);
 }
 
-template <typename T, bool CG, int N>
+template <typename T, bool CG, int N, int TH>
 __device__ __forceinline__ void y_tile(const PassArgs& a, Cx<T>* Sm, long long plane, int item) {
-  constexpr int EY = fast_points(N, false), TY = N / EY, LY = kThreads / TY;
+  constexpr int EY = fast_points(N, false), TY = N / EY, LY = TH / TY;
   const int tid = threadIdx.x;
   const int line = tid % LY, t = tid / LY;
   LineCtx<T, K_C2C, false, CG> c;
@@ -67,13 +66,14 @@ __device__ __forceinline__ void y_tile(const PassArgs& a, Cx<T>* Sm, long long p
 
 // sync[0]: ticket counter, sync[1]: error flag, sync[2 + p]: phase-1 tiles
 // of plane p completed.  The host zeroes it before every launch.
-template <typename T, int KINDX, bool XFIRST, int NX, int NY>
-__global__ void __launch_bounds__(kThreads, 1) fused_xy_kernel(const __grid_constant__ FusedArgs f) {
+// 256 threads: two CTAs an SM (at most 128 registers); 512: one.
+template <typename T, int KINDX, bool XFIRST, int NX, int NY, int TH>
+__global__ void __launch_bounds__(TH, TH == 256 ? 2 : 1) fused_xy_kernel(const __grid_constant__ FusedArgs f) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ long long s_ticket;
   Cx<T>* Sm = reinterpret_cast<Cx<T>*>(smem_raw);
-  constexpr int LX = kThreads / (NX / fast_points(NX, true));
-  constexpr int LY = kThreads / (NY / fast_points(NY, false));
+  constexpr int LX = TH / (NX / fast_points(NX, true));
+  constexpr int LY = TH / (NY / fast_points(NY, false));
   const int items_x = (int)((f.ax.nlines + LX - 1) / LX);
   const int items_y = (f.ay.nlines + LY - 1) / LY;
   const int n1 = XFIRST ? items_x : items_y;  // phase-1 tiles per plane
@@ -113,9 +113,9 @@ __global__ void __launch_bounds__(kThreads, 1) fused_xy_kernel(const __grid_cons
     }
     if (phase1) {
       if constexpr (XFIRST)
-        x_tile<T, KINDX, false, NX>(f.ax, Sm, plane, item);
+        x_tile<T, KINDX, false, NX, TH>(f.ax, Sm, plane, item);
       else
-        y_tile<T, false, NY>(f.ay, Sm, plane, item);
+        y_tile<T, false, NY, TH>(f.ay, Sm, plane, item);
       __threadfence();
       __syncthreads();
       if (threadIdx.x == 0) atomicAdd(sync + 2 + plane, 1);
@@ -123,30 +123,30 @@ __global__ void __launch_bounds__(kThreads, 1) fused_xy_kernel(const __grid_cons
       if (threadIdx.x == 0) bounded_wait(sync + 2 + plane, n1, kSpinLimit, sync + 1, 1);
       __syncthreads();
       if constexpr (XFIRST)
-        y_tile<T, true, NY>(f.ay, Sm, plane, item);
+        y_tile<T, true, NY, TH>(f.ay, Sm, plane, item);
       else
-        x_tile<T, KINDX, true, NX>(f.ax, Sm, plane, item);
+        x_tile<T, KINDX, true, NX, TH>(f.ax, Sm, plane, item);
     }
   }
 }
 
-template <int NX, int NY>
+template <int NX, int NY, int TH>
 constexpr size_t smem_bytes(int cbytes) {
-  constexpr long long ex = fast_smem_entries(NX, kThreads / (NX / fast_points(NX, true)));
-  constexpr long long ey = fast_smem_entries(NY, kThreads / (NY / fast_points(NY, false)));
+  constexpr long long ex = fast_smem_entries(NX, TH / (NX / fast_points(NX, true)));
+  constexpr long long ey = fast_smem_entries(NY, TH / (NY / fast_points(NY, false)));
   return (size_t)(ex > ey ? ex : ey) * (size_t)cbytes;
 }
 
-template <typename T, int KINDX, bool XFIRST, int NX, int NY>
+template <typename T, int KINDX, bool XFIRST, int NX, int NY, int TH>
 cudaError_t launch(const FusedArgs& f, cudaStream_t stream) {
-  auto kern = fused_xy_kernel<T, KINDX, XFIRST, NX, NY>;
-  const size_t smem = smem_bytes<NX, NY>((int)sizeof(Cx<T>));
+  auto kern = fused_xy_kernel<T, KINDX, XFIRST, NX, NY, TH>;
+  const size_t smem = smem_bytes<NX, NY, TH>((int)sizeof(Cx<T>));
   static int grid = 0;  // resident CTAs, per instantiation, first use
   if (grid == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0, dev = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TH, smem);
     if (e != cudaSuccess) return e;
     e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -157,7 +157,7 @@ cudaError_t launch(const FusedArgs& f, cudaStream_t stream) {
   const size_t sync_bytes = (size_t)(f.nplanes + 2) * sizeof(int);
   cudaError_t e = cudaMemsetAsync(f.sync, 0, sync_bytes, stream);
   if (e != cudaSuccess) return e;
-  kern<<<grid, kThreads, smem, stream>>>(f);
+  kern<<<grid, TH, smem, stream>>>(f);
   add_launches(1);
   return cudaGetLastError();
 }

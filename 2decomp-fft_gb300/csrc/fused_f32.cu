@@ -7,13 +7,21 @@ namespace gbfft {
 
 namespace {
 
+template <int N, int TH>
+cudaError_t launch_nt(int kindx, bool x_first, const FusedArgs& f, cudaStream_t s) {
+  if (kindx == K_C2C)
+    return x_first ? fused::launch<float, K_C2C, true, N, N, TH>(f, s)
+                   : fused::launch<float, K_C2C, false, N, N, TH>(f, s);
+  if (kindx == K_R2C && x_first) return fused::launch<float, K_R2C, true, N, N, TH>(f, s);
+  if (kindx == K_C2R && !x_first) return fused::launch<float, K_C2R, false, N, N, TH>(f, s);
+  return cudaErrorNotSupported;
+}
+
 template <int N>
 cudaError_t launch_n(int kindx, bool x_first, const FusedArgs& f, cudaStream_t s) {
-  if (kindx == K_C2C)
-    return x_first ? fused::launch<float, K_C2C, true, N, N>(f, s) : fused::launch<float, K_C2C, false, N, N>(f, s);
-  if (kindx == K_R2C && x_first) return fused::launch<float, K_R2C, true, N, N>(f, s);
-  if (kindx == K_C2R && !x_first) return fused::launch<float, K_C2R, false, N, N>(f, s);
-  return cudaErrorNotSupported;
+  if (f.threads == 256) return launch_nt<N, 256>(kindx, x_first, f, s);
+  if (f.threads == 512) return launch_nt<N, 512>(kindx, x_first, f, s);
+  return cudaErrorInvalidValue;
 }
 
 bool size_ok(int nx, int ny) { return nx == ny && (nx == 256 || nx == 512 || nx == 1024); }

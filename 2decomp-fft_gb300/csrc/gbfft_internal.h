@@ -60,6 +60,13 @@ struct PassArgs {
                    // 3: split-precision tensor-core kernel
   int pair_vec;    // r2c/c2r on strided lines: the two real lines of a pair
                    // are adjacent and 8-byte aligned (read/write as one pair)
+  int pipe;        // fast == 1: 0 = one-shot kernel, 2 or 3 = pipelined
+                   // persistent kernel with that many tile buffers
+  int csize;       // fast == 1, one-shot: 0, or launch CTAs in clusters of
+                   // csize neighbours (co-scheduled: their row segments
+                   // reach DRAM together)
+  int csync;       // with csize: the CTAs of a cluster start with a
+                   // cluster barrier
   int radix[kMaxStages];
 };
 
@@ -84,7 +91,11 @@ __host__ __device__ constexpr int fast_nst(int n, int e) {
 __host__ __device__ constexpr int fast_radix(int n, int e, int s) {
   return e == 32 ? (s == 0 ? 32 : n / 32) : (s < ilog2c(n) / 4 ? 16 : (1 << (ilog2c(n) % 4)));
 }
-constexpr int kFastMaxThreadsF32 = 512;
+// Thread limits of the power-of-two kernel, launched with one CTA per SM
+// guaranteed: 16 points a thread at most 64 registers (1024 threads, FP32),
+// 32 points a thread at most 128 (512 threads).  Smaller tiles of the same
+// kernel still run several CTAs per SM.
+constexpr int kFastMaxThreadsF32 = 1024;
 constexpr int kFastMaxThreadsF64 = 256;
 // Mixed-radix lengths with a compile-time-planned kernel (fft_mixed.cuh):
 // n = R0 * R1, R0 <= R1 <= 32, the most balanced such split.
@@ -104,12 +115,20 @@ cudaError_t launch_mixed_f32(int kind, bool contiguous, const PassArgs& a, cudaS
 bool split_length(int n);
 int split_lines_per_cta(int n, bool contiguous);
 cudaError_t launch_split_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+// Pipelined persistent passes (fft_pipe.cuh): FP32 lines of 256, 512, 1024
+// points; all tile buffers of a CTA within kPipeSmemLimit bytes.
+constexpr size_t kPipeSmemLimit = 226 * 1024;
+bool pipe_length(int n);
+cudaError_t launch_pipe_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 cudaError_t launch_mixed_f64(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 
 // Thread limit of the power-of-two kernel for E points a thread.
 __host__ __device__ constexpr int fast_max_threads(int e, int prec_bytes) {
-  return e == 32 ? 256 : (prec_bytes == 4 ? kFastMaxThreadsF32 : kFastMaxThreadsF64);
+  return e == 32 ? (prec_bytes == 4 ? 512 : 256) : (prec_bytes == 4 ? kFastMaxThreadsF32 : kFastMaxThreadsF64);
 }
+// Thread limit of the pipelined kernel (one CTA per SM, registers for E
+// points plus the copy loop's addressing).
+__host__ __device__ constexpr int pipe_max_threads(int e) { return e == 32 ? 256 : 512; }
 // Shared-memory entries of one power-of-two tile of L lines: the exchange
 // buffer, or for c2r the staged half spectra (n/2+1 per real line).
 __host__ __device__ constexpr long long fast_smem_entries(int n, int L) {
@@ -128,14 +147,16 @@ struct FusedArgs {
   PassArgs ax;
   PassArgs ay;
   long long nplanes;
-  int* sync;  // nplanes + 2 ints: ticket, error flag, per-plane counters
+  int* sync;    // nplanes + 2 ints: ticket, error flag, per-plane counters
+  int threads;  // threads per CTA: 256 or 512 (ax.L, ay.L follow from it)
 };
 
 // True when a fused x/y kernel exists for these lengths (x first or y
 // first, x kind K_C2C / K_R2C / K_C2R).
 bool fused_supported(int prec_bytes, int kindx, bool x_first, int nx, int ny);
-// Threads per CTA of the fused kernel (one tile of L = 512 / (n / 16) lines).
-constexpr int kFusedThreads = 512;
+// Default threads per CTA of the fused kernel (a tile of L = threads / (n / E)
+// lines).
+constexpr int kFusedThreads = 256;
 // Enqueue a fused x/y pass (zeroes f.sync first).
 cudaError_t launch_fused(int prec_bytes, int kindx, bool x_first, const FusedArgs& f, cudaStream_t stream);
 

@@ -64,6 +64,10 @@ SIGNATURES = {
     "gbfft_batch_destroy": (_i, [_vp]),
     "gbfft_engine_set_profiling": (_i, [_vp, _i]),
     "gbfft_engine_set_tile": (_i, [_vp, _i, _i]),
+    "gbfft_engine_set_pipeline": (_i, [_vp, _i, _i]),
+    "gbfft_engine_get_pipeline": (_i, [_vp, _ip]),
+    "gbfft_engine_set_cluster": (_i, [_vp, _i, _i, _i]),
+    "gbfft_engine_get_cluster": (_i, [_vp, _ip, _ip]),
     "gbfft_engine_set_fusion": (_i, [_vp, _i]),
     "gbfft_engine_status": (_i, [_vp]),
     "gbfft_tune_cache_path": (_i, [ctypes.c_char_p]),
@@ -221,6 +225,28 @@ class Engine:
             kind = PASS_NAMES.index(kind)
         check(lib().gbfft_engine_set_tile(self.h, int(kind), int(lines)))
 
+
+    def set_pipeline(self, kind, depth):
+        """Pipelined persistent kernel for a pass kind (name or GBFFT_PASS_*):
+        depth 2 or 3 tile buffers, 0 = one CTA per tile."""
+        k = PASS_NAMES.index(kind) if isinstance(kind, str) else int(kind)
+        check(lib().gbfft_engine_set_pipeline(self.h, k, int(depth)))
+
+    def set_cluster(self, kind, ctas, sync=True):
+        """Launch a pass kind's CTAs in clusters of ctas (2, 4, 8; 0 = off),
+        with a cluster barrier at the start when sync."""
+        k = PASS_NAMES.index(kind) if isinstance(kind, str) else int(kind)
+        check(lib().gbfft_engine_set_cluster(self.h, k, int(ctas), int(bool(sync))))
+
+    def cluster(self):
+        c, s = (ctypes.c_int * len(PASS_NAMES))(), (ctypes.c_int * len(PASS_NAMES))()
+        check(lib().gbfft_engine_get_cluster(self.h, c, s))
+        return {k: (c[i], s[i]) for i, k in enumerate(PASS_NAMES)}
+
+    def pipeline(self):
+        d = (ctypes.c_int * len(PASS_NAMES))()
+        check(lib().gbfft_engine_get_pipeline(self.h, d))
+        return dict(zip(PASS_NAMES, d))
     def set_fusion(self, enable):
         """Fuse the x and y passes of each z-plane into one kernel (default on)."""
         check(lib().gbfft_engine_set_fusion(self.h, int(bool(enable))))

@@ -9,6 +9,12 @@ creation (tune_cache.txt beside this file, or $GBFFT_TUNE_CACHE):
   * the tile shape (lines per CTA) of every pass kind          -> r2c, c2r,
                                                                   c2c_x, c2c_y,
                                                                   c2c_z, xy_fused
+  * launch form: one CTA per tile, the same in clusters of 2, 4 or 8
+    neighbouring CTAs (with or without a start barrier), or a
+    persistent kernel streaming tiles through 2 or 3 shared-memory
+    buffers                                                    -> cl_<pass>,
+                                                                  cls_<pass>,
+                                                                  pipe_<pass>
   * pass fusion: x and y passes of each z-plane in one kernel  -> fuse
 
 The measured step is the benchmark's: one r2c then one c2r, per-pass device
@@ -35,6 +41,9 @@ DEFAULT_SHAPES = [
     (4, 1, 256, 256, 256), (8, 1, 64, 64, 64),
 ]
 TILES = [1, 2, 4, 8, 16, 32]
+# launch forms: (pipeline depth, (cluster CTAs, start barrier)); one-shot
+# kernels plain or in clusters, or the pipelined kernel with 2 or 3 buffers
+LAUNCHES = [(0, (0, 0)), (0, (2, 0)), (0, (2, 1)), (0, (4, 1)), (0, (8, 1)), (2, (0, 0)), (3, (0, 0))]
 
 
 def measure(eng, x, s, y, steps=6, warm=2):
@@ -81,25 +90,36 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
             eng.set_plan(2, ez)
         times, _ = measure(eng, x, s, y)
         tiles = {}
+        pipes = {}
+        clusters = {}
         total = 0.0
         for kind, t0 in times.items():
-            bt, bl = t0, 0
-            for L in TILES:
-                try:
-                    eng.set_tile(kind, L)
-                except gbfft.GbfftError:
-                    continue
-                t = measure(eng, x, s, y, steps=4, warm=1)[0].get(kind, t0)
-                if t < bt:
-                    bt, bl = t, L
-                eng.set_tile(kind, 0)
+            bt, bl, bp = t0, 0, 0
+            bc = (0, 0)
+            for depth, clus in LAUNCHES if kind != "xy_fused" else [(0, (0, 0))]:
+                eng.set_pipeline(kind, depth)
+                eng.set_cluster(kind, *clus)
+                for L in [0] + TILES:
+                    try:
+                        eng.set_tile(kind, L)
+                    except gbfft.GbfftError:
+                        continue
+                    t = measure(eng, x, s, y, steps=4, warm=1)[0].get(kind, t0)
+                    if t < bt:
+                        bt, bl, bp, bc = t, L, depth, clus
+                    eng.set_tile(kind, 0)
+            eng.set_pipeline(kind, 0)
+            eng.set_cluster(kind, 0, 0)
             tiles[kind] = bl
+            pipes[kind] = bp
+            clusters[kind] = bc
             mult = 2 if kind.startswith("c2c") else 1
             total += mult * bt
-        log("  plan e_y=%s e_z=%s: est %.4f ms %s" % (ey, ez, total, tiles))
+        log("  plan e_y=%s e_z=%s: est %.4f ms tiles %s pipes %s clusters %s" % (ey, ez, total, tiles, pipes,
+                                                                                clusters))
         if best is None or total < best[0]:
-            best = (total, ey, ez, tiles)
-    total, ey, ez, tiles = best
+            best = (total, ey, ez, tiles, pipes, clusters)
+    total, ey, ez, tiles, pipes, clusters = best
     if ey:
         eng.set_plan(1, ey)
     if ez:
@@ -107,6 +127,12 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     for kind, L in tiles.items():
         if L:
             eng.set_tile(kind, L)
+    for kind, d in pipes.items():
+        if d:
+            eng.set_pipeline(kind, d)
+    for kind, c in clusters.items():
+        if c[0]:
+            eng.set_cluster(kind, *c)
     _, step_plain = measure(eng, x, s, y)
     fuse = 0
     eng.set_fusion(True)
@@ -124,6 +150,14 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     for kind, L in sorted(tiles.items()):
         if L:
             fields.append("%s=%d" % (kind, L))
+    for kind, d in sorted(pipes.items()):
+        if d:
+            fields.append("pipe_%s=%d" % (kind, d))
+    for kind, c in sorted(clusters.items()):
+        if c[0]:
+            fields.append("cl_%s=%d" % (kind, c[0]))
+            if c[1]:
+                fields.append("cls_%s=1" % kind)
     return " ".join(fields), min(step_plain, step_fused if fuse else step_plain)
 
 
@@ -136,7 +170,9 @@ def main():
     gbfft.lib()
     gbfft.set_tune_cache("")  # measure from the built-in choices
     lines = ["# GB300 tuning cache written by tune.py: prec format nx ny nz key=value ...",
-             "# keys: fuse, e_y/e_z (points per thread of strided plans), lines per CTA per pass"]
+             "# keys: fuse, e_y/e_z (points per thread of strided plans), lines per CTA per pass,",
+             "# pipe_<pass> (tile buffers of the pipelined kernel), cl_<pass> / cls_<pass> (cluster",
+             "# launch: CTAs a cluster / start barrier)"]
     for shp in shapes:
         print("shape", shp, flush=True)
         line, ms = tune_shape(*shp)

@@ -177,6 +177,25 @@ int gbfft_engine_set_profiling(gbfft_engine_t engine, int enable);
  * the kernel's thread or shared-memory limit. */
 int gbfft_engine_set_tile(gbfft_engine_t engine, int kind, int lines_per_cta);
 
+/* Pipelining of one pass kind (GBFFT_PASS_*), FP32 axes of 256, 512 or
+ * 1024 points with a power-of-two plan: depth 2 or 3 runs the pass as a
+ * persistent kernel whose CTAs stream tiles through that many shared-memory
+ * buffers with asynchronous copies (the loads of the next tiles in flight
+ * while one is transformed); 0 (default) runs one CTA per tile.  Other
+ * passes ignore it.  gbfft_engine_get_pipeline fills GBFFT_PASS_KINDS ints. */
+int gbfft_engine_set_pipeline(gbfft_engine_t engine, int kind, int depth);
+int gbfft_engine_get_pipeline(gbfft_engine_t engine, int* depth);
+
+/* Cluster launch of one pass kind (GBFFT_PASS_*) on its power-of-two
+ * one-shot kernel: ctas 2, 4 or 8 launches neighbouring CTAs (neighbouring
+ * lines) as thread-block clusters, which the GPU co-schedules, and sync = 1
+ * starts every CTA with a cluster barrier, so that the row segments that
+ * the CTAs of a cluster read from the same rows of a strided axis arrive at
+ * DRAM together.  0 (default) launches plain CTAs.  gbfft_engine_get_cluster
+ * fills GBFFT_PASS_KINDS ints each. */
+int gbfft_engine_set_cluster(gbfft_engine_t engine, int kind, int ctas, int sync);
+int gbfft_engine_get_cluster(gbfft_engine_t engine, int* ctas, int* sync);
+
 /* Pass fusion: 1 (default) lets the engine run the x and y passes of each
  * z-plane in one kernel where a fused kernel exists for the lengths; 0 runs
  * one kernel per axis. */
@@ -186,7 +205,10 @@ int gbfft_engine_set_fusion(gbfft_engine_t engine, int enable);
  * Engines apply a tuning cache at creation: a text file (default
  * tune_cache.txt in the package directory, or $GBFFT_TUNE_CACHE; "" = none)
  * with lines "prec format nx ny nz key=value ...": per pass kind the lines
- * per CTA (r2c c2r c2c_x c2c_y c2c_z xy_fused), fuse=0/1, and e_y / e_z,
+ * per CTA (r2c c2r c2c_x c2c_y c2c_z xy_fused), the pipeline depth per pass
+ * kind (pipe_r2c, pipe_c2r, pipe_c2c_x, ...), the cluster launch per pass
+ * kind (cl_<pass> = CTAs a cluster, cls_<pass> = 1 for the start barrier),
+ * fuse=0/1, and e_y / e_z,
  * the points per thread of the strided y / z plan (16: radix 16, 16, ...;
  * 32: two radix-32 stages) for axes of 512 or 1024 points.  The tuner
  * (2decomp-fft_gb300/tune.py) measures the choices and writes the file. */
