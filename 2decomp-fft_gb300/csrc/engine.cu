@@ -238,6 +238,7 @@ void load_tune_locked() {
       const std::string k = kv.substr(0, eq);
       const int v = std::atoi(kv.c_str() + eq + 1);
       if (k == "fuse") t.fuse = v;
+      else if (k == "e_x") t.e[0] = v;
       else if (k == "e_y") t.e[1] = v;
       else if (k == "e_z") t.e[2] = v;
       for (int i = 0; i < GBFFT_PASS_KINDS; ++i) {
@@ -434,7 +435,7 @@ void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int ki
     a.nst = 0;
     a.tw = p.d_twf;
     a.fast = 1;
-    const int fe = contiguous ? fast_points(p.n, true) : p.fast_e;
+    const int fe = p.fast_e;  // only axis 0 runs contiguous lines
     a.tpl = p.n / fe;
     a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L, fe);
     a.first_fused = 1;
@@ -596,6 +597,7 @@ void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
     if (!fast_length(px.a.n) || !fast_length(py.a.n)) continue;
     if (px.a.fast != 1 || py.a.fast != 1 || px.a.pipe || py.a.pipe || px.a.csize || py.a.csize) continue;
     if (e->ax[1].fast_e != fast_points(py.a.n, false)) continue;  // the fused kernel's y plan
+    if (e->ax[0].fast_e != fast_points(px.a.n, true)) continue;   // and its x plan
     if (!fused_supported(e->prec, px.kind, xfirst, px.a.n, py.a.n)) continue;
     long long per_plane;
     if (px.kind == K_C2C) {
@@ -816,7 +818,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
                                              " does not fit one shared-memory tile at this precision");
     }
     e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
-    if (d > 0 && fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
+    if (fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
     if (form == GBFFT_FORM_SPLIT) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
     int rc = upload_twiddles(e->ax[d], prec);
     if (rc != GBFFT_OK) {
@@ -1021,7 +1023,7 @@ int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
   const bool contig_pass = (kind == GBFFT_PASS_C2C_X) ||
                            ((kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R) &&
                             e->format == GBFFT_PHYSICAL_IN_X);
-  const int fe = contig_pass ? fast_points(p.n, true) : p.fast_e;
+  const int fe = p.fast_e;
   int tpl = fast ? p.n / fe : p.tpl;
   const int maxt = fast ? fast_max_threads(fe, e->prec) : kMaxThreads;
   if (!fast) {
@@ -1107,7 +1109,7 @@ int gbfft_tune_cache_path(const char* path) {
 
 int gbfft_engine_set_plan(gbfft_engine_t e, int axis, int points) {
   if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
-  if (axis < 1 || axis > 2) return fail(GBFFT_ERR_INVALID, "only the strided axes (1, 2) have plan choices");
+  if (axis < 0 || axis > 2) return fail(GBFFT_ERR_INVALID, "bad axis");
   AxisPlan& p = e->ax[axis];
   if (e->form == GBFFT_FORM_SPLIT) return fail(GBFFT_ERR_UNSUPPORTED, "the split form has one plan");
   if (!fast_has_alt(p.n)) return fail(GBFFT_ERR_UNSUPPORTED, "this axis length has one plan");

@@ -186,11 +186,12 @@ cudaError_t launch_ne(const PassArgs& a, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-// Strided lines of 512 and 1024 points have two plans: 32 points a thread
-// (two stages, the default) or 16 (three stages); a.tpl says which.
+// Lines of 512 and 1024 points have two plans: 32 points a thread (two
+// stages; the strided default; a contiguous line is then one warp) or 16
+// (three stages; the contiguous default); a.tpl says which.
 template <typename T, int KIND, bool CONTIG, int N>
 cudaError_t launch_n(const PassArgs& a, cudaStream_t stream) {
-  if constexpr (!CONTIG && (N == 512 || N == 1024)) {
+  if constexpr (N == 512 || N == 1024) {
     if (a.tpl == N / 16) return launch_ne<T, KIND, CONTIG, N, 16>(a, stream);
     return launch_ne<T, KIND, CONTIG, N, 32>(a, stream);
   } else {

@@ -61,7 +61,7 @@ cudaError_t launch_e(const PassArgs& a, cudaStream_t s) {
 
 template <int KIND, bool CONTIG, int N>
 cudaError_t launch_n(const PassArgs& a, cudaStream_t s) {
-  if constexpr (!CONTIG && (N == 512 || N == 1024)) {
+  if constexpr (N == 512 || N == 1024) {
     if (a.tpl == N / 16) return launch_e<KIND, CONTIG, N, 16>(a, s);
     return launch_e<KIND, CONTIG, N, 32>(a, s);
   } else {

@@ -4,8 +4,8 @@ For each grid shape it measures, on the GPU at hand, the choices an engine
 can make and writes the fastest into the tuning cache that engines read at
 creation (tune_cache.txt beside this file, or $GBFFT_TUNE_CACHE):
 
-  * the radix plan of strided axes of 512 or 1024 points: 16 points per
-    thread (radix 16 stages) or 32 (two radix-32 stages)      -> e_y, e_z
+  * the radix plan of axes of 512 or 1024 points: 16 points per thread
+    (radix 16 stages) or 32 (two radix-32 stages)             -> e_x, e_y, e_z
   * the tile shape (lines per CTA) of every pass kind          -> r2c, c2r,
                                                                   c2c_x, c2c_y,
                                                                   c2c_z, xy_fused
@@ -41,6 +41,7 @@ DEFAULT_SHAPES = [
     (4, 1, 256, 256, 256), (8, 1, 64, 64, 64),
 ]
 TILES = [1, 2, 4, 8, 16, 32]
+MARGIN = 0.99
 # launch forms: (pipeline depth, (cluster CTAs, start barrier)); one-shot
 # kernels plain or in clusters, or the pipelined kernel with 2 or 3 buffers
 LAUNCHES = [(0, (0, 0)), (0, (2, 0)), (0, (2, 1)), (0, (4, 1)), (0, (8, 1)), (2, (0, 0)), (3, (0, 0))]
@@ -79,11 +80,13 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     s = eng.empty_spectral()
     y = eng.empty_physical()
     opts = {}
-    for axis, n in ((1, ny), (2, nz)):
+    for axis, n in ((0, nx), (1, ny), (2, nz)):
         opts[axis] = [16, 32] if n in (512, 1024) else [None]
     eng.set_fusion(False)
     best = None
-    for ey, ez in itertools.product(opts[1], opts[2]):
+    for ex, ey, ez in itertools.product(opts[0], opts[1], opts[2]):
+        if ex:
+            eng.set_plan(0, ex)
         if ey:
             eng.set_plan(1, ey)
         if ez:
@@ -93,10 +96,18 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
         pipes = {}
         clusters = {}
         total = 0.0
+        pts = eng.tuning()["points"]
         for kind, t0 in times.items():
             bt, bl, bp = t0, 0, 0
             bc = (0, 0)
-            for depth, clus in LAUNCHES if kind != "xy_fused" else [(0, (0, 0))]:
+            # launch forms exist for the compile-time power-of-two kernels
+            # (the pipelined one in FP32 only)
+            axis = {"c2c_x": 0, "c2c_y": 1, "c2c_z": 2}.get(kind, 0 if fmt == 1 else 2)
+            if kind == "xy_fused" or not pts[axis]:
+                forms = [(0, (0, 0))]
+            else:
+                forms = [f for f in LAUNCHES if prec == 4 or f[0] == 0]
+            for depth, clus in forms:
                 eng.set_pipeline(kind, depth)
                 eng.set_cluster(kind, *clus)
                 for L in [0] + TILES:
@@ -105,7 +116,8 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
                     except gbfft.GbfftError:
                         continue
                     t = measure(eng, x, s, y, steps=4, warm=1)[0].get(kind, t0)
-                    if t < bt:
+                    # a choice other than the built-in one must win by 1 %
+                    if t < bt and t < t0 * MARGIN:
                         bt, bl, bp, bc = t, L, depth, clus
                     eng.set_tile(kind, 0)
             eng.set_pipeline(kind, 0)
@@ -115,11 +127,13 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
             clusters[kind] = bc
             mult = 2 if kind.startswith("c2c") else 1
             total += mult * bt
-        log("  plan e_y=%s e_z=%s: est %.4f ms tiles %s pipes %s clusters %s" % (ey, ez, total, tiles, pipes,
-                                                                                clusters))
+        log("  plan e_x=%s e_y=%s e_z=%s: est %.4f ms tiles %s pipes %s clusters %s" % (
+            ex, ey, ez, total, tiles, pipes, clusters))
         if best is None or total < best[0]:
-            best = (total, ey, ez, tiles, pipes, clusters)
-    total, ey, ez, tiles, pipes, clusters = best
+            best = (total, ex, ey, ez, tiles, pipes, clusters)
+    total, ex, ey, ez, tiles, pipes, clusters = best
+    if ex:
+        eng.set_plan(0, ex)
     if ey:
         eng.set_plan(1, ey)
     if ez:
@@ -143,6 +157,8 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
                                                     "" if "xy_fused" in times_f else " (no fused kernel)"))
     eng.close()
     fields = ["%d %d %d %d %d" % (prec, fmt, nx, ny, nz), "fuse=%d" % fuse]
+    if ex:
+        fields.append("e_x=%d" % ex)
     if ey:
         fields.append("e_y=%d" % ey)
     if ez:
@@ -170,7 +186,7 @@ def main():
     gbfft.lib()
     gbfft.set_tune_cache("")  # measure from the built-in choices
     lines = ["# GB300 tuning cache written by tune.py: prec format nx ny nz key=value ...",
-             "# keys: fuse, e_y/e_z (points per thread of strided plans), lines per CTA per pass,",
+             "# keys: fuse, e_x/e_y/e_z (points per thread of the axis plans), lines per CTA per pass,",
              "# pipe_<pass> (tile buffers of the pipelined kernel), cl_<pass> / cls_<pass> (cluster",
              "# launch: CTAs a cluster / start barrier)"]
     for shp in shapes:

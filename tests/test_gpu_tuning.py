@@ -37,6 +37,50 @@ def test_strided_plans_give_the_same_transform(fmt, ey, ez):
     e.close()
 
 
+@pytest.mark.parametrize("fmt", [1, 3])
+@pytest.mark.parametrize("nx", [512, 1024])
+@pytest.mark.parametrize("ex", [16, 32])
+def test_contiguous_plans_give_the_same_transform(fmt, nx, ex):
+    # axis 0 (contiguous lines) with 16 points a thread or 32 (one warp a
+    # line): r2c / c2r along x for PHYSICAL_IN_X, c2c along x for _Z
+    import gbfft
+    ny, nz = 34, 20
+    x = np.random.default_rng(nx + ex + fmt).standard_normal((nz, ny, nx))
+    e = gbfft.Engine(fmt, nx, ny, nz, prec=gbfft.PREC_SINGLE)
+    e.set_plan(0, ex)
+    assert e.tuning()["points"][0] == ex
+    xd = torch.from_numpy(x.astype(np.float32)).cuda()
+    s = e.empty_spectral()
+    e.r2c(xd, s)
+    assert rel(s.cpu().numpy(), O.fft3d_r2c(x, fmt)) <= 2e-6
+    y = e.empty_physical()
+    e.c2r(s, y)
+    assert rel(y.cpu().numpy() / (nx * ny * nz), x) <= 2e-6
+    c = x + 1j * np.random.default_rng(1).standard_normal(x.shape)
+    cd = torch.from_numpy(c.astype(np.complex64)).cuda()
+    o = torch.empty_like(cd)
+    e.c2c(cd, o, -1)
+    assert rel(o.cpu().numpy(), O.fft3d_c2c(c.copy(), fmt, -1)) <= 2e-6
+    e.close()
+
+
+@pytest.mark.parametrize("ex", [16, 32])
+def test_contiguous_plans_double_precision(ex):
+    import gbfft
+    nx, ny, nz = 1024, 6, 5
+    x = np.random.default_rng(ex).standard_normal((nz, ny, nx))
+    e = gbfft.Engine(1, nx, ny, nz, prec=gbfft.PREC_DOUBLE)
+    e.set_plan(0, ex)
+    xd = torch.from_numpy(x).cuda()
+    s = e.empty_spectral()
+    e.r2c(xd, s)
+    assert rel(s.cpu().numpy(), O.fft3d_r2c(x, 1)) <= 1e-12
+    y = e.empty_physical()
+    e.c2r(s, y)
+    assert rel(y.cpu().numpy() / (nx * ny * nz), x) <= 1e-12
+    e.close()
+
+
 def test_tile_shapes_give_the_same_transform():
     import gbfft
     nx, ny, nz = 256, 64, 48
