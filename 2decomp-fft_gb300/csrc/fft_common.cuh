@@ -348,10 +348,13 @@ struct LineCtx {
   }
 
   // c2r input staging: the two half spectra of this line pair (n/2+1 points
-  // each) in shared memory, slot j of half h at sstage(h (n/2+1) + j).
+  // each) in shared memory, interleaved: pair slot j holds (X1[j], X2[j]),
+  // so that the Hermitian gather reads both with one 16-byte load (FP32).
+  struct alignas(16) Pair {
+    C a, b;
+  };
   __device__ __forceinline__ int sstage(int j) const {
-    const int a = CONTIG ? line * (N + 2) + j : j * L + line;
-    return a + (a >> 4);
+    return CONTIG ? line * (N / 2 + 1) + j : j * L + line;
   }
   // NN, TPL: the line length and threads per line, known at compile time so
   // that every load is issued before the first shared-memory store.
@@ -360,6 +363,7 @@ struct LineCtx {
     constexpr int h = NN / 2 + 1;
     constexpr int J = (h + TPL - 1) / TPL;
     const C* s = reinterpret_cast<const C*>(src);
+    Pair* P = reinterpret_cast<Pair*>(S);
     C a[J], b[J];
 #pragma unroll
     for (int i = 0; i < J; ++i) {
@@ -371,20 +375,17 @@ struct LineCtx {
 #pragma unroll
     for (int i = 0; i < J; ++i) {
       const int j = t + i * TPL;
-      if (j < h) {
-        S[sstage(j)] = a[i];
-        S[sstage(h + j)] = b[i];
-      }
+      if (j < h) P[sstage(j)] = Pair{a[i], b[i]};
     }
   }
   // Point n of the complex line z = x1 + i x2 built from the staged half
   // spectra by the Hermitian extension (src/fft_generic.f90:318-330),
   // conjugated for the inverse-by-conjugation.
   __device__ __forceinline__ C sgather_c2r(const C* S, int n) const {
-    const int h = N / 2 + 1;
     const bool low = 2 * n <= N;
     const int m = low ? n : N - n;
-    C x1 = S[sstage(m)], x2 = S[sstage(h + m)];
+    const Pair p = reinterpret_cast<const Pair*>(S)[sstage(m)];
+    C x1 = p.a, x2 = p.b;
     if (!low) {
       x1.y = -x1.y;
       x2.y = -x2.y;

@@ -84,9 +84,11 @@ __device__ __forceinline__ void issue_tile(const PassArgs& a, Cx<T>* S, long lon
       }
     }
   } else {
-    // c2r: the two half spectra of each line pair, slot sstage(hh h + j);
-    // on strided axes neighbouring lanes take the two lines of a pair and
-    // then neighbouring pairs, i.e. consecutive x positions
+    // c2r: the two half spectra of each line pair, interleaved: X_hh[j] is
+    // half hh of pair slot j (CONTIG: line (N/2+1) + j, strided: j L + line,
+    // as LineCtx::sstage); on strided axes neighbouring lanes take the two
+    // lines of a pair and then neighbouring pairs, i.e. consecutive x
+    // positions
     const C* src = reinterpret_cast<const C*>(a.src);
     constexpr int H = N / 2 + 1;
     for (int e = tid; e < 2 * H * L; e += nthreads) {
@@ -105,8 +107,7 @@ __device__ __forceinline__ void issue_tile(const PassArgs& a, Cx<T>* S, long lon
       const long long cl = u0 + line;
       if (cl >= nl) continue;
       const long long r = 2 * cl + hh;
-      const int jj = hh * H + j;
-      C* d = S + pad_slot(CONTIG ? line * (N + 2) + jj : jj * L + line);
+      C* d = S + 2 * (CONTIG ? line * H + j : j * L + line) + hh;
       if (r < a.real_lines) {
         const long long off = CONTIG ? r * a.s_src_l + j : r + v * a.s_src_l + (long long)j * a.s_src_n;
         cp_async<sizeof(C)>(d, src + off);

@@ -132,7 +132,9 @@ __host__ __device__ constexpr int pipe_max_threads(int e) { return e == 32 ? 256
 // Shared-memory entries of one power-of-two tile of L lines: the exchange
 // buffer, or for c2r the staged half spectra (n/2+1 per real line).
 __host__ __device__ constexpr long long fast_smem_entries(int n, int L) {
-  return (long long)(n + 2) * L + (((long long)(n + 2) * L) >> 4) + 1;
+  // rounded up to an even count: buffers laid end to end stay 16-byte
+  // aligned (the c2r staging reads 16-byte pairs)
+  return ((long long)(n + 2) * L + (((long long)(n + 2) * L) >> 4) + 2) & ~1ll;
 }
 
 cudaError_t launch_fast_f32_c2c(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
