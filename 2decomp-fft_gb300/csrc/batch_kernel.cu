@@ -72,7 +72,7 @@ __device__ __forceinline__ void run_tile(const BatchDesc& D, Cx<T>* Sm, long lon
     constexpr int E = fast_points(N, CONTIG);
     Cx<T> v[E];
     fast::run_stages<N, E, 0>(c, Sm, v);
-    if constexpr (KIND == K_R2C) c.store_r2c(Sm);
+    if constexpr (KIND == K_R2C) c.store_r2c_pairs(Sm);
   }
 }
 

@@ -397,6 +397,32 @@ struct LineCtx {
     return cmk<C>(x1.x - x2.y, -(x1.y + x2.x));
   }
 
+  // r2c output in pair slots (the c2r staging layout): slot k holds
+  // (Z[k], Z[n-k]) for k <= n/2, so that the split below reads both with one
+  // 16-byte load (FP32).  put_r2c stores point j of the transformed line.
+  __device__ __forceinline__ void put_r2c(C* S, int j, C v) const {
+    Pair* P = reinterpret_cast<Pair*>(S);
+    if (2 * j <= N) {
+      P[sstage(j)].a = v;
+      if (j == 0 || 2 * j == N) P[sstage(j)].b = v;
+    } else {
+      P[sstage(N - j)].b = v;
+    }
+  }
+  __device__ __forceinline__ void store_r2c_pairs(const C* S) const {
+    if (!valid) return;
+    const Pair* P = reinterpret_cast<const Pair*>(S);
+    C* d = reinterpret_cast<C*>(dst);
+    const T h = T(0.5);
+#pragma unroll 1
+    for (int k = t; 2 * k <= N; k += tpl) {
+      const Pair p = P[sstage(k)];
+      const C zk = p.a, zm = p.b;
+      d[db0 + k * dsn] = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
+      if (has1) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
+    }
+  }
+
   // r2c output: separate the two half spectra held in shared memory,
   // X1 = (Z_k + conj Z_{n-k}) / 2, X2 = (Z_k - conj Z_{n-k}) / (2i).
   __device__ __forceinline__ void store_r2c(const C* S) const {

@@ -112,7 +112,12 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
         for (int r = 0; r < R; ++r) c.gstore(base + r * NS, v[m * R + r]);
       }
     } else {
-      if constexpr (!FIRST) stage_barrier<WL>();
+      // r2c's last stage writes pair slots, which straddle the regions of
+      // neighbouring lines: the whole CTA must be done reading
+      if constexpr (!FIRST) {
+        if constexpr (LAST && KIND == K_R2C) __syncthreads();
+        else stage_barrier<WL>();
+      }
       // (SMEM0: the first stage synchronised after its shared-memory reads)
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
@@ -120,7 +125,10 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
         const int k = b & (NS - 1);
         const int base = (b - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) Sm[c.sidx(base + r * NS)] = v[m * R + r];
+        for (int r = 0; r < R; ++r) {
+          if constexpr (LAST && KIND == K_R2C) c.put_r2c(Sm, base + r * NS, v[m * R + r]);
+          else Sm[c.sidx(base + r * NS)] = v[m * R + r];
+        }
       }
       // the r2c split after the last stage reads other lines' points
       if constexpr (LAST) __syncthreads();
@@ -147,7 +155,7 @@ __global__ void __launch_bounds__(fast_max_threads(E, sizeof(T)), 1)
   c.init(a);
   Cx<T> v[E];
   run_stages<N, E, 0>(c, Sm, v);
-  if constexpr (KIND == K_R2C) c.store_r2c(Sm);
+  if constexpr (KIND == K_R2C) c.store_r2c_pairs(Sm);
 }
 
 template <typename T, int KIND, bool CONTIG, int N, int E>

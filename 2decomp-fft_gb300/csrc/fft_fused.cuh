@@ -50,7 +50,7 @@ __device__ __forceinline__ void x_tile(const PassArgs& a, Cx<T>* Sm, long long p
   c.init_at(a, t, line, first + (long long)item * LX + line, 0, first + per_plane);
   Cx<T> v[EX];
   run_stages<N, EX, 0>(c, Sm, v);
-  if constexpr (KIND == K_R2C) c.store_r2c(Sm);
+  if constexpr (KIND == K_R2C) c.store_r2c_pairs(Sm);
 }
 
 template <typename T, bool CG, int N, int TH>

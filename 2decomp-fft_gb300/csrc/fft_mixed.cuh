@@ -183,10 +183,10 @@ __device__ __forceinline__ void run_mixed(const Ctx& c, C* Sm) {
     __syncthreads();
     if (act) {
 #pragma unroll
-      for (int r = 0; r < R1; ++r) Sm[c.sidx(t + r * R0)] = v[r];
+      for (int r = 0; r < R1; ++r) c.put_r2c(Sm, t + r * R0, v[r]);
     }
     __syncthreads();
-    c.store_r2c(Sm);
+    c.store_r2c_pairs(Sm);
   } else {
     if (act) {
 #pragma unroll

@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(pipe_max_threads(E), 1)
     c.init_at(a, t, line, ub * L + line, v, a.nlines);
     C x[E];
     fast::run_stages<N, E, 0, LineCtx<T, KIND, CONTIG>, C, true>(c, Sm, x);
-    if constexpr (KIND == K_R2C) c.store_r2c(Sm);
+    if constexpr (KIND == K_R2C) c.store_r2c_pairs(Sm);
     __syncthreads();
     cur = (cur + 1) % D;
   }
