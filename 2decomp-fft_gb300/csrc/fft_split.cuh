@@ -13,15 +13,22 @@
 // lo = fp16(v - hi) (about 22 bits together), and three of the four cross
 // products are accumulated in FP32:
 //     Y = Fh Xh + Fh Xl + Fl Xh        (Fl Xl, ~2^-22 relative, dropped)
-// with the large and the small products in separate accumulators (see
-// mma_stage16).
 // Before the split each butterfly's 16 inputs are scaled by a power of two
 // that brings their largest component just under 1 (exact, undone on the
 // outputs), which keeps hi inside FP16's range and lo above its subnormals.
 //
-// Lines sit in shared memory throughout (two ping-pong buffers): a load phase
-// reads global memory, every stage reads one buffer and writes the other,
-// a store phase writes global memory.
+// The tensor cores align the terms of one product-sum to the largest and
+// drop the bits below FP32's precision, so a chain of six products into one
+// accumulator loses a few units in the last place at every step: the two
+// hi*hi products start from zero in accumulators of their own, the four
+// small corrections share a third, and the three are added with rounding.
+//
+// Fragment layout (PTX m16n8k16, .row.col): lane (g = lane / 4, q = lane % 4)
+// holds column g of B at rows 2q, 2q+1, 2q+8, 2q+9 and, of the result, rows
+// g and g+8 at columns 2q and 2q+1.  A group of 8 butterflies is one B
+// matrix: on contiguous lines 8 neighbouring butterflies of one line, on
+// strided lines the same butterfly of 8 neighbouring lines (so the loads of
+// a group are 64-byte row segments either way).
 #pragma once
 
 #include <cuda_fp16.h>
@@ -35,22 +42,22 @@ using namespace dev;
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ void mma16816(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+__device__ __forceinline__ void mma16816(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
       "{%0,%1,%2,%3};\n"
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ unsigned pack2(__half lo_index, __half hi_index) {
-  __half2 h = __halves2half2(lo_index, hi_index);
-  return *reinterpret_cast<unsigned*>(&h);
-}
+__device__ __forceinline__ unsigned as_u32(__half2 h) { return *reinterpret_cast<unsigned*>(&h); }
 
-__device__ __forceinline__ void split1(float v, __half& hi, __half& lo) {
-  hi = __float2half_rn(v);
-  lo = __float2half_rn(v - __half2float(hi));
+// hi / lo halves of (v0, v1), packed with v0 in the low half
+__device__ __forceinline__ void split2(float v0, float v1, unsigned& hi, unsigned& lo) {
+  const __half2 h = __floats2half2_rn(v0, v1);
+  const float2 b = __half22float2(h);
+  hi = as_u32(h);
+  lo = as_u32(__floats2half2_rn(v0 - b.x, v1 - b.y));
 }
 
 // W16^m = exp(-2 pi i m / 16), m = 0..15
@@ -62,136 +69,73 @@ __device__ __forceinline__ float2 w16(int m) {
 }
 
 // A fragments of F16 (rows r = output, columns k = input) for this lane:
-// Frh/Frl: real part hi/lo, Fih/Fil: imaginary part hi/lo, and the negated
-// imaginary part for the real output.
+// real part hi / lo, imaginary part hi / lo.
 struct DftFrag {
-  unsigned rh[4], rl[4], ih[4], il[4], nih[4], nil[4];
+  unsigned rh[4], rl[4], ih[4], il[4];
 };
 
 __device__ __forceinline__ void dft16_frag(DftFrag& f, int lane) {
-  const int g = lane >> 2, t = lane & 3;
+  const int g = lane >> 2, q = lane & 3;
   const int rows[4] = {g, g + 8, g, g + 8};
-  const int cols[4] = {2 * t, 2 * t, 2 * t + 8, 2 * t + 8};
+  const int cols[4] = {2 * q, 2 * q, 2 * q + 8, 2 * q + 8};
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const float2 w0 = w16(rows[i] * cols[i]), w1 = w16(rows[i] * (cols[i] + 1));
-    __half h0, l0, h1, l1;
-    split1(w0.x, h0, l0);
-    split1(w1.x, h1, l1);
-    f.rh[i] = pack2(h0, h1);
-    f.rl[i] = pack2(l0, l1);
-    split1(w0.y, h0, l0);
-    split1(w1.y, h1, l1);
-    f.ih[i] = pack2(h0, h1);
-    f.il[i] = pack2(l0, l1);
-    f.nih[i] = pack2(__hneg(h0), __hneg(h1));
-    f.nil[i] = pack2(__hneg(l0), __hneg(l1));
+    split2(w0.x, w1.x, f.rh[i], f.rl[i]);
+    split2(w0.y, w1.y, f.ih[i], f.il[i]);
   }
 }
 
-// One radix-16 Stockham stage on the tensor cores, shared buffer A -> B.
-// Butterfly b (0 <= b < n/16) of a line reads points b + k n/16 (k = 0..15),
-// multiplies by W_{16 NS}^{(b mod NS) k} (stage-major table, entry
-// NS - 1 + (k - 1) NS + b mod NS), transforms, and writes point
-// (b - b mod NS) 16 + b mod NS + r NS for output r.
-template <int N, class Ctx>
-__device__ __forceinline__ void mma_stage16(const Ctx& c, const DftFrag& F, const float2* A, float2* B, int NS,
-                                            int lines) {
-  constexpr int NB = N / 16;
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const int nwarps = kThreads / 32;
-  const int g = lane >> 2, t = lane & 3;
-  const int groups = lines * (NB / 8);
-  const int ks[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
-  for (int G = warp; G < groups; G += nwarps) {
-    const int line = G / (NB / 8);
-    const int b = (G % (NB / 8)) * 8 + g;  // this lane's butterfly (column g)
-    const int kb = b & (NS - 1);
-    float2 x[4];
+// One group of 8 radix-16 butterflies: x[j] is this lane's input at row
+// k = 2q, 2q+1, 2q+8, 2q+9 (j = 0..3) of column g; y[i] the output at row
+// (i < 2 ? g : g + 8), column 2q + (i & 1).  All lanes of the warp call it.
+__device__ __forceinline__ void mma_group(const DftFrag& F, const float2 (&x)[4], float2 (&y)[4], int lane) {
+  const int q = lane & 3;
+  // power-of-two scale of this column's butterfly (the 4 lanes with this g)
+  float m = 0.f;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      x[j] = A[c.sidx_at(line, b + ks[j] * NB)];
-      if (NS > 1 && ks[j] > 0) x[j] = cmul(x[j], c.twiddle((NS - 1) + (ks[j] - 1) * NS + kb));
-    }
-    // power-of-two scale of this butterfly (the 4 lanes with the same g)
-    float m = 0.f;
+  for (int j = 0; j < 4; ++j) m = fmaxf(m, fmaxf(fabsf(x[j].x), fabsf(x[j].y)));
+  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+  int e = 0;
+  if (m > 0.f) frexpf(m, &e);
+  e = max(-125, min(e, 126));  // keep both 2^-e and 2^e normal floats
+  const float sc = ldexpf(1.f, -e), unsc = ldexpf(1.f, e);
+  unsigned rh0, rl0, rh1, rl1, ih0, il0, ih1, il1;
+  split2(x[0].x * sc, x[1].x * sc, rh0, rl0);
+  split2(x[2].x * sc, x[3].x * sc, rh1, rl1);
+  split2(x[0].y * sc, x[1].y * sc, ih0, il0);
+  split2(x[2].y * sc, x[3].y * sc, ih1, il1);
+  const unsigned neg = 0x80008000u;  // -Xi for the real part
+  float yr[4], yi[4];
+  {
+    float a[4] = {0.f, 0.f, 0.f, 0.f}, b[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
+    mma16816(a, F.rh, rh0, rh1);              // Fr Xr, hi hi
+    mma16816(b, F.ih, ih0 ^ neg, ih1 ^ neg);  // -Fi Xi, hi hi
+    mma16816(c, F.rh, rl0, rl1);
+    mma16816(c, F.rl, rh0, rh1);
+    mma16816(c, F.ih, il0 ^ neg, il1 ^ neg);
+    mma16816(c, F.il, ih0 ^ neg, ih1 ^ neg);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) m = fmaxf(m, fmaxf(fabsf(x[j].x), fabsf(x[j].y)));
-    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
-    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
-    int e = 0;
-    if (m > 0.f) frexpf(m, &e);
-    e = max(-125, min(e, 126));  // keep both 2^-e and 2^e normal floats
-    const float sc = ldexpf(1.f, -e), unsc = ldexpf(1.f, e);
-    __half rh[4], rl[4], ih[4], il[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      split1(x[j].x * sc, rh[j], rl[j]);
-      split1(x[j].y * sc, ih[j], il[j]);
-    }
-    const unsigned brh[2] = {pack2(rh[0], rh[1]), pack2(rh[2], rh[3])};
-    const unsigned brl[2] = {pack2(rl[0], rl[1]), pack2(rl[2], rl[3])};
-    const unsigned bih[2] = {pack2(ih[0], ih[1]), pack2(ih[2], ih[3])};
-    const unsigned bil[2] = {pack2(il[0], il[1]), pack2(il[2], il[3])};
-    // Yr = Fr Xr - Fi Xi,  Yi = Fi Xr + Fr Xi; each as hi*hi + hi*lo + lo*hi.
-    // The tensor cores align the terms of one product-sum to the largest
-    // and drop the bits below FP32's precision, so a chain of six products
-    // into one accumulator loses a few units in the last place at every
-    // step.  The two hi*hi products start from zero in accumulators of
-    // their own, the four small corrections share a third, and the three
-    // are added with rounding at the end.
-    float ar[4] = {0.f, 0.f, 0.f, 0.f}, br[4] = {0.f, 0.f, 0.f, 0.f}, cr[4] = {0.f, 0.f, 0.f, 0.f};
-    float ai[4] = {0.f, 0.f, 0.f, 0.f}, bi[4] = {0.f, 0.f, 0.f, 0.f}, ci[4] = {0.f, 0.f, 0.f, 0.f};
-    mma16816(ar, F.rh, brh);
-    mma16816(br, F.nih, bih);
-    mma16816(cr, F.rh, brl);
-    mma16816(cr, F.rl, brh);
-    mma16816(cr, F.nih, bil);
-    mma16816(cr, F.nil, bih);
-    mma16816(ai, F.ih, brh);
-    mma16816(bi, F.rh, bih);
-    mma16816(ci, F.ih, brl);
-    mma16816(ci, F.il, brh);
-    mma16816(ci, F.rh, bil);
-    mma16816(ci, F.rl, bih);
-    float yr[4], yi[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      yr[i] = (ar[i] + br[i]) + cr[i];
-      yi[i] = (ai[i] + bi[i]) + ci[i];
-    }
-    // outputs: rows r = g, g + 8; columns (butterflies) 2t, 2t + 1; each
-    // column's scale lives in lanes 4 * column
-    const float u0 = __shfl_sync(0xffffffffu, unsc, 8 * t), u1 = __shfl_sync(0xffffffffu, unsc, 8 * t + 4);
-    const int bq = (G % (NB / 8)) * 8;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int r = (i < 2) ? g : g + 8;
-      const int col = 2 * t + (i & 1);
-      const float u = (i & 1) ? u1 : u0;
-      const int bb = bq + col;
-      const int k = bb & (NS - 1);
-      B[c.sidx_at(line, (bb - k) * 16 + k + r * NS)] = make_float2(yr[i] * u, yi[i] * u);
-    }
+    for (int i = 0; i < 4; ++i) yr[i] = (a[i] + b[i]) + c[i];
   }
-}
-
-// Plain radix-R stage (the last factor 2 or 4), shared buffer A -> B.
-template <int N, int R, class Ctx>
-__device__ __forceinline__ void plain_stage(const Ctx& c, const float2* A, float2* B, int NS, int lines) {
-  constexpr int NB = N / R;
-  for (int w = threadIdx.x; w < lines * NB; w += kThreads) {
-    const int line = w / NB, b = w % NB;
-    float2 v[R];
+  {
+    float a[4] = {0.f, 0.f, 0.f, 0.f}, b[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
+    mma16816(a, F.ih, rh0, rh1);  // Fi Xr, hi hi
+    mma16816(b, F.rh, ih0, ih1);  // Fr Xi, hi hi
+    mma16816(c, F.ih, rl0, rl1);
+    mma16816(c, F.il, rh0, rh1);
+    mma16816(c, F.rh, il0, il1);
+    mma16816(c, F.rl, ih0, ih1);
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = A[c.sidx_at(line, b + r * NB)];
-    const int k = b & (NS - 1);
+    for (int i = 0; i < 4; ++i) yi[i] = (a[i] + b[i]) + c[i];
+  }
+  // each output column's scale lives in lanes 4 * column
+  const float u0 = __shfl_sync(0xffffffffu, unsc, 8 * q), u1 = __shfl_sync(0xffffffffu, unsc, 8 * q + 4);
 #pragma unroll
-    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], c.twiddle((NS - 1) + (r - 1) * NS + k));
-    dftp<R>(v);
-#pragma unroll
-    for (int r = 0; r < R; ++r) B[c.sidx_at(line, (b - k) * R + k + r * NS)] = v[r];
+  for (int i = 0; i < 4; ++i) {
+    const float u = (i & 1) ? u1 : u0;
+    y[i] = make_float2(yr[i] * u, yi[i] * u);
   }
 }
 
