@@ -169,16 +169,25 @@ int upload_table(void** dst, const std::vector<double>& t, int prec) {
   return GBFFT_OK;
 }
 
+// Radices of an axis's compile-time plan (power of two: fast_e points a
+// thread; balanced non-power-of-two plan when fast_e = gen_points(n); the
+// two-stage mixed-radix plan otherwise); empty when the axis has none.
+std::vector<int> plan_radices(const AxisPlan& p) {
+  std::vector<int> radices;
+  if (fast_length(p.n)) {
+    for (int s = 0; s < fast_nst(p.n, p.fast_e); ++s) radices.push_back(fast_radix(p.n, p.fast_e, s));
+  } else if (gen_length(p.n) && p.fast_e == gen_points(p.n)) {
+    for (int s = 0; gen_radix(p.n, s) > 0; ++s) radices.push_back(gen_radix(p.n, s));
+  } else if (mixed_length(p.n)) {
+    radices = {mixed_r0(p.n), p.n / mixed_r0(p.n)};
+  }
+  return radices;
+}
+
 int upload_twiddles(AxisPlan& p, int prec) {
   int rc = upload_table(&p.d_tw, twiddles(p.n), prec);
-  if (rc == GBFFT_OK && fast_length(p.n)) {
-    std::vector<int> radices;
-    for (int s = 0; s < fast_nst(p.n, p.fast_e); ++s) radices.push_back(fast_radix(p.n, p.fast_e, s));
-    rc = upload_table(&p.d_twf, stage_twiddles(radices), prec);
-  } else if (rc == GBFFT_OK && mixed_length(p.n)) {
-    const int r0 = mixed_r0(p.n);
-    rc = upload_table(&p.d_twf, stage_twiddles({r0, p.n / r0}), prec);
-  }
+  const std::vector<int> radices = plan_radices(p);
+  if (rc == GBFFT_OK && !radices.empty()) rc = upload_table(&p.d_twf, stage_twiddles(radices), prec);
   return rc;
 }
 
@@ -404,6 +413,30 @@ int mixed_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int 
   return L;
 }
 
+// Lines a CTA of the balanced non-power-of-two kernel: contiguous lines 128
+// threads a CTA (at least one line); strided lines enough for 64-byte row
+// segments and about 512 threads; within the thread and 100 KB shared-memory
+// limits.
+int gen_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int forced_L) {
+  const int e = gen_points(n), tpl = n / e, maxt = gen_max_threads(e, prec);
+  int L;
+  if (forced_L > 0) {
+    L = forced_L;
+  } else if (contiguous) {
+    L = tpl >= 128 ? 1 : 128 / tpl;
+  } else {
+    L = 512 / tpl;
+    if (L > 32) L = 32;
+    const int min_l = (int)(64 / (2 * prec));
+    if (L < min_l) L = min_l;
+  }
+  while (L > 1 && L * tpl > maxt) --L;
+  while (L > 1 && (size_t)fast_smem_entries(n, L) * 2 * prec > (forced_L > 0 ? 200 : 100) * 1024) --L;
+  if (L < 1) L = 1;
+  if (forced_L <= 0 && L > 1 && nlines < L) L = (int)nlines;
+  return L;
+}
+
 void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind, int forced_L,
                bool split = false, int pipe = 0, int csize = 0, int csync = 0) {
   if (split && split_length(p.n)) {
@@ -417,6 +450,17 @@ void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int ki
     a.last_fused = 0;
     (void)forced_L;
     (void)kind;
+    return;
+  }
+  if (gen_length(p.n) && p.fast_e == gen_points(p.n)) {
+    a.n = p.n;
+    a.nst = 0;
+    a.tw = p.d_twf;
+    a.fast = 4;
+    a.tpl = p.n / p.fast_e;
+    a.L = gen_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L);
+    a.first_fused = 1;
+    a.last_fused = kind != K_R2C;
     return;
   }
   if (mixed_length(p.n)) {
@@ -818,8 +862,11 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
                                              " does not fit one shared-memory tile at this precision");
     }
     e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
+    if (gen_length(lens[d])) e->ax[d].fast_e = gen_points(lens[d]);
     if (fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
-    if (form == GBFFT_FORM_SPLIT) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
+    if (gen_length(lens[d]) && (tune.e[d] == gen_points(lens[d]) || tune.e[d] == 2))
+      e->ax[d].fast_e = tune.e[d];
+    if (form == GBFFT_FORM_SPLIT && split_length(lens[d])) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
     int rc = upload_twiddles(e->ax[d], prec);
     if (rc != GBFFT_OK) {
       release(e);
@@ -1011,6 +1058,15 @@ int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
   else
     axis = kind - GBFFT_PASS_C2C_X;
   const AxisPlan& p = e->ax[axis];
+  if (gen_length(p.n) && p.fast_e == gen_points(p.n)) {
+    const int tpl_g = p.n / p.fast_e;
+    if (lines * tpl_g > gen_max_threads(p.fast_e, e->prec))
+      return fail(GBFFT_ERR_INVALID, "tile exceeds the kernel's thread limit");
+    if ((size_t)fast_smem_entries(p.n, lines) * 2 * (size_t)e->prec > 200 * 1024)
+      return fail(GBFFT_ERR_INVALID, "tile exceeds the shared-memory limit");
+    e->tile_L[kind] = lines;
+    return GBFFT_OK;
+  }
   if (mixed_length(p.n)) {
     const int tpl_m = p.n / mixed_r0(p.n);
     if (lines * tpl_m > 256) return fail(GBFFT_ERR_INVALID, "tile exceeds the kernel's thread limit");
@@ -1111,17 +1167,21 @@ int gbfft_engine_set_plan(gbfft_engine_t e, int axis, int points) {
   if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
   if (axis < 0 || axis > 2) return fail(GBFFT_ERR_INVALID, "bad axis");
   AxisPlan& p = e->ax[axis];
-  if (e->form == GBFFT_FORM_SPLIT) return fail(GBFFT_ERR_UNSUPPORTED, "the split form has one plan");
-  if (!fast_has_alt(p.n)) return fail(GBFFT_ERR_UNSUPPORTED, "this axis length has one plan");
-  if (points != 16 && points != 32) return fail(GBFFT_ERR_INVALID, "points per thread must be 16 or 32");
+  if (e->form == GBFFT_FORM_SPLIT && split_length(p.n))
+    return fail(GBFFT_ERR_UNSUPPORTED, "the split form has one plan");
+  if (gen_length(p.n)) {
+    if (points != gen_points(p.n) && points != 2)
+      return fail(GBFFT_ERR_INVALID, "points per thread must be the balanced plan's or 2 (two-stage plan)");
+  } else {
+    if (!fast_has_alt(p.n)) return fail(GBFFT_ERR_UNSUPPORTED, "this axis length has one plan");
+    if (points != 16 && points != 32) return fail(GBFFT_ERR_INVALID, "points per thread must be 16 or 32");
+  }
   if (p.fast_e == points) return GBFFT_OK;
   void* old = p.d_twf;
   const int old_e = p.fast_e;
   p.fast_e = points;
   p.d_twf = nullptr;
-  std::vector<int> radices;
-  for (int s = 0; s < fast_nst(p.n, points); ++s) radices.push_back(fast_radix(p.n, points, s));
-  int rc = upload_table(&p.d_twf, stage_twiddles(radices), e->prec);
+  int rc = upload_table(&p.d_twf, stage_twiddles(plan_radices(p)), e->prec);
   if (rc != GBFFT_OK) {
     p.fast_e = old_e;
     p.d_twf = old;
@@ -1139,7 +1199,8 @@ int gbfft_engine_get_tuning(gbfft_engine_t e, int* fuse, int* tiles, int* points
   if (tiles)
     for (int k = 0; k < GBFFT_PASS_KINDS; ++k) tiles[k] = e->tile_L[k];
   if (points)
-    for (int d = 0; d < 3; ++d) points[d] = fast_length(e->ax[d].n) ? e->ax[d].fast_e : 0;
+    for (int d = 0; d < 3; ++d)
+      points[d] = (fast_length(e->ax[d].n) || gen_length(e->ax[d].n)) ? e->ax[d].fast_e : 0;
   return GBFFT_OK;
 }
 

@@ -202,6 +202,8 @@ cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous, const Pa
     if (prec_bytes != 4) return cudaErrorInvalidValue;
     return launch_pipe_f32(kind, contiguous, a, stream);
   }
+  if (a.fast == 4) return prec_bytes == 4 ? launch_gen_f32(kind, contiguous, a, stream)
+                                          : launch_gen_f64(kind, contiguous, a, stream);
   if (a.fast == 3) {
     if (prec_bytes != 4) return cudaErrorInvalidValue;
     return launch_split_f32(kind, contiguous, a, stream);

@@ -196,6 +196,138 @@ template <int R, typename C> __device__ __forceinline__ void dftp(C* v) {
 }
 
 // ---------------------------------------------------------------------------
+// Butterflies of any 7-smooth radix up to 32 (and products of those), built
+// at compile time as a two-level Cooley-Tukey split R = P * Q in registers,
+// with the internal twiddles W_R^{n2 k1} evaluated by a constexpr
+// sine/cosine (argument reduced exactly on the rational angle, Taylor series
+// in double).
+// ---------------------------------------------------------------------------
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr double taylor_sin(double x) {
+  double t = x, s = x;
+  for (int k = 1; k < 14; ++k) {
+    t *= -x * x / ((2.0 * k) * (2.0 * k + 1));
+    s += t;
+  }
+  return s;
+}
+constexpr double taylor_cos(double x) {
+  double t = 1, s = 1;
+  for (int k = 1; k < 14; ++k) {
+    t *= -x * x / ((2.0 * k - 1) * (2.0 * k));
+    s += t;
+  }
+  return s;
+}
+struct SinCos {
+  double s, c;
+};
+// sin and cos of 2 pi m / d: reduced to [0, pi/4] by exact rational steps
+// (f -> 1 - f, 1/2 - f, 1/4 - f), then Taylor series.
+constexpr SinCos sincos_2pi(long long m, long long d) {
+  m %= d;
+  if (m < 0) m += d;
+  double ss = 1, sc = 1;
+  bool swap = false;
+  if (2 * m > d) {
+    m = d - m;
+    ss = -1;
+  }
+  if (4 * m > d) {
+    m = d - 2 * m;
+    d = 2 * d;
+    sc = -sc;
+  }
+  if (8 * m > d) {
+    m = d - 4 * m;
+    d = 4 * d;
+    swap = true;
+  }
+  const double x = kTwoPi * (double)m / (double)d;
+  double s = taylor_sin(x), c = taylor_cos(x);
+  if (swap) {
+    const double t = s;
+    s = c;
+    c = t;
+  }
+  return {ss * s, sc * c};
+}
+
+template <int R, int M>
+__device__ __forceinline__ constexpr double root_c() {
+  constexpr SinCos v = sincos_2pi(M, R);
+  return v.c;
+}
+template <int R, int M>
+__device__ __forceinline__ constexpr double root_s() {
+  constexpr SinCos v = sincos_2pi(M, R);
+  return v.s;
+}
+
+template <int B, int E, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    static_for<B + 1, E>(f);
+  }
+}
+
+constexpr bool special_radix(int r) {
+  return r == 2 || r == 3 || r == 4 || r == 5 || r == 7 || r == 8 || r == 16 || r == 32;
+}
+constexpr int pick_p(int r) {
+  for (int p : {16, 8, 4, 5, 3, 7, 2})
+    if (r % p == 0 && r != p) return p;
+  return r;
+}
+
+// Forward DFT of size R in registers, natural order in and out.
+template <int R, typename C>
+__device__ __forceinline__ void dftg(C* v) {
+  if constexpr (R == 1) {
+  } else if constexpr (special_radix(R)) {
+    dftp<R>(v);
+  } else {
+    using T = decltype(C::x);
+    constexpr int P = pick_p(R), Q = R / P;
+    C a[R];
+    // n = Q n1 + n2, k = k1 + P k2: DFT_P over n1, twiddle W_R^{n2 k1}
+    static_for<0, Q>([&](auto I2) {
+      constexpr int n2 = decltype(I2)::value;
+      C t[P];
+      static_for<0, P>([&](auto I1) {
+        constexpr int n1 = decltype(I1)::value;
+        t[n1] = v[Q * n1 + n2];
+      });
+      dftg<P>(t);
+      static_for<0, P>([&](auto K1) {
+        constexpr int k1 = decltype(K1)::value;
+        constexpr int e = (n2 * k1) % R;
+        if constexpr (e == 0)
+          a[n2 * P + k1] = t[k1];
+        else
+          a[n2 * P + k1] = cmul(t[k1], cmk<C>(T(root_c<R, e>()), T(-root_s<R, e>())));
+      });
+    });
+    // DFT_Q over n2 for each k1
+    static_for<0, P>([&](auto K1) {
+      constexpr int k1 = decltype(K1)::value;
+      C u[Q];
+      static_for<0, Q>([&](auto I2) {
+        constexpr int n2 = decltype(I2)::value;
+        u[n2] = a[n2 * P + k1];
+      });
+      dftg<Q>(u);
+      static_for<0, Q>([&](auto K2) {
+        constexpr int k2 = decltype(K2)::value;
+        v[k1 + P * k2] = u[k2];
+      });
+    });
+  }
+}
+
+
+// ---------------------------------------------------------------------------
 // Per-thread view of one line: shared-memory slots and global addressing.
 // ---------------------------------------------------------------------------
 // CG: read sources through L2 only (ld.global.cg), for data other CTAs of

@@ -29,12 +29,12 @@ namespace fast {
 
 using namespace dev;
 
-template <int N, int E_>
+template <int N_, int E_>
 struct P2Plan {
-  static constexpr int E = E_;
-  static constexpr int NST = fast_nst(N, E);
-  static constexpr int TPL = N / E;
-  __host__ __device__ static constexpr int radix(int s) { return fast_radix(N, E, s); }
+  static constexpr int N = N_, E = E_;
+  static constexpr int NST = fast_nst(N_, E_);
+  static constexpr int TPL = N_ / E_;
+  __host__ __device__ static constexpr int radix(int s) { return fast_radix(N_, E_, s); }
   __host__ __device__ static constexpr int ns(int s) {
     int v = 1;
     for (int i = 0; i < s; ++i) v *= radix(i);
@@ -52,13 +52,17 @@ template <bool WARP_LOCAL> __device__ __forceinline__ void stage_barrier() {
 // SMEM0: stage 0 reads its points from Sm (already filled by the caller:
 // natural order for c2c / r2c, the staged half spectra for c2r) instead of
 // global memory.
-template <int N, int E, int S, class Ctx, class C, bool SMEM0 = false>
-__device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
-  using P = P2Plan<N, E>;
+// A compile-time plan P (P2Plan, GenPlan): line length P::N, P::E points a
+// thread, P::TPL threads a line, P::NST stages of radix P::radix(s) after
+// P::ns(s) points; every radix divides E.
+template <class P, int S, class Ctx, class C, bool SMEM0 = false>
+__device__ __forceinline__ void run_plan(const Ctx& c, C* Sm, C (&v)[P::E]) {
+  constexpr int N = P::N, E = P::E;
   constexpr int KIND = Ctx::kind;
-  constexpr bool WL = Ctx::contiguous && P::TPL <= 32;
+  // warp-local barriers need every line inside one warp: TPL must divide 32
+  constexpr bool WL = Ctx::contiguous && P::TPL <= 32 && 32 % P::TPL == 0;
   if constexpr (S < P::NST) {
-    constexpr int R = P::radix(S), NS = P::ns(S), MB = P::E / R, NB = N / R, TPL = P::TPL;
+    constexpr int R = P::radix(S), NS = P::ns(S), MB = E / R, NB = N / R, TPL = P::TPL;
     constexpr bool FIRST = (S == 0), LAST = (S == P::NST - 1);
     const int t = c.t;
     if constexpr (FIRST && KIND == K_C2R) {
@@ -95,18 +99,18 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
 #pragma unroll
     for (int m = 0; m < MB; ++m) {
       const int b = t + m * TPL;
-      const int k = b & (NS - 1);
+      const int k = b % NS;
       if constexpr (NS > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) v[m * R + r] = cmul(v[m * R + r], c.twiddle((NS - 1) + (r - 1) * NS + k));
       }
-      dftp<R>(&v[m * R]);
+      dftg<R>(&v[m * R]);
     }
     if constexpr (LAST && KIND != K_R2C) {
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         const int b = t + m * TPL;
-        const int k = b & (NS - 1);
+        const int k = b % NS;
         const int base = (b - k) * R + k;
 #pragma unroll
         for (int r = 0; r < R; ++r) c.gstore(base + r * NS, v[m * R + r]);
@@ -122,7 +126,7 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         const int b = t + m * TPL;
-        const int k = b & (NS - 1);
+        const int k = b % NS;
         const int base = (b - k) * R + k;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -134,9 +138,27 @@ __device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
       if constexpr (LAST) __syncthreads();
       else stage_barrier<WL>();
     }
-    run_stages<N, E, S + 1, Ctx, C, SMEM0>(c, Sm, v);
+    run_plan<P, S + 1, Ctx, C, SMEM0>(c, Sm, v);
   }
 }
+
+template <int N, int E, int S, class Ctx, class C, bool SMEM0 = false>
+__device__ __forceinline__ void run_stages(const Ctx& c, C* Sm, C (&v)[E]) {
+  run_plan<P2Plan<N, E>, S, Ctx, C, SMEM0>(c, Sm, v);
+}
+
+// Plans for 7-smooth lengths that are not powers of two, chosen so that
+// every radix divides E and all TPL threads of a line work in every stage:
+// 243 = 9 9 3 (E 9), 270 = 15 6 3 (E 30), 360 = 10 6 6 (E 30),
+// 384 = 8 8 6 (E 24), 400 = 20 20 (E 20).
+template <int N_, int E_, int R0, int R1, int R2 = 1>
+struct GenPlan {
+  static constexpr int N = N_, E = E_, TPL = N_ / E_;
+  static constexpr int NST = R2 > 1 ? 3 : 2;
+  __host__ __device__ static constexpr int radix(int s) { return s == 0 ? R0 : (s == 1 ? R1 : R2); }
+  __host__ __device__ static constexpr int ns(int s) { return s == 0 ? 1 : (s == 1 ? R0 : R0 * R1); }
+  static_assert(R0 * R1 * R2 == N_ && E_ % R0 == 0 && E_ % R1 == 0 && E_ % R2 == 0, "bad plan");
+};
 
 // 16 points a thread, FP32: up to 1024 threads, i.e. at most 64 registers a
 // thread, so a 512-thread strided tile still runs two CTAs per SM and a

@@ -57,7 +57,8 @@ struct PassArgs {
   int first_fused; // stage 0 reads global memory directly
   int last_fused;  // last stage writes global memory directly
   int fast;        // 1: compile-time power-of-two kernel, 2: mixed-radix kernel,
-                   // 3: split-precision tensor-core kernel
+                   // 3: split-precision tensor-core kernel, 4: balanced
+                   // non-power-of-two plan
   int pair_vec;    // r2c/c2r on strided lines: the two real lines of a pair
                    // are adjacent and 8-byte aligned (read/write as one pair)
   int pipe;        // fast == 1: 0 = one-shot kernel, 2 or 3 = pipelined
@@ -110,6 +111,29 @@ __host__ __device__ constexpr bool mixed_length(int n) {
          n == 384 || n == 400;
 }
 cudaError_t launch_mixed_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+// Non-power-of-two lengths with a balanced compile-time plan (fft_gen.cuh,
+// fast::GenPlan): E points a thread, n / E threads a line.
+__host__ __device__ constexpr bool gen_length(int n) {
+  return n == 243 || n == 270 || n == 360 || n == 384 || n == 400;
+}
+__host__ __device__ constexpr int gen_points(int n) {
+  return n == 243 ? 9 : (n == 270 || n == 360) ? 30 : n == 384 ? 24 : n == 400 ? 20 : 0;
+}
+// the plan's radices, stage by stage (0 after the last)
+__host__ __device__ constexpr int gen_radix(int n, int s) {
+  return n == 243 ? (s < 2 ? 9 : s == 2 ? 3 : 0)
+       : n == 270 ? (s == 0 ? 15 : s == 1 ? 6 : s == 2 ? 3 : 0)
+       : n == 360 ? (s == 0 ? 10 : s < 3 ? 6 : 0)
+       : n == 384 ? (s < 2 ? 8 : s == 2 ? 6 : 0)
+       : n == 400 ? (s < 2 ? 20 : 0) : 0;
+}
+// thread limit: E <= 16 at most 64 registers (1024 threads, FP32), more
+// points at most 128 (512 threads); FP64 256 threads
+__host__ __device__ constexpr int gen_max_threads(int e, int prec_bytes) {
+  return prec_bytes == 8 ? 256 : (e <= 16 ? 1024 : 512);
+}
+cudaError_t launch_gen_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
+cudaError_t launch_gen_f64(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 // Split-precision tensor-core passes (fft_split.cuh): FP32 lines of 256,
 // 512, 1024 points, 256-thread CTAs of split_lines_per_cta lines.
 bool split_length(int n);

@@ -1,0 +1,8 @@
+// Balanced-plan non-power-of-two passes (fft_gen.cuh), FP64.
+#include "fft_gen.cuh"
+
+namespace gbfft {
+cudaError_t launch_gen_f64(int kind, bool contiguous, const PassArgs& a, cudaStream_t s) {
+  return gen::launch<double>(kind, contiguous, a, s);
+}
+}  // namespace gbfft

@@ -5,7 +5,9 @@ can make and writes the fastest into the tuning cache that engines read at
 creation (tune_cache.txt beside this file, or $GBFFT_TUNE_CACHE):
 
   * the radix plan of axes of 512 or 1024 points: 16 points per thread
-    (radix 16 stages) or 32 (two radix-32 stages)             -> e_x, e_y, e_z
+    (radix 16 stages) or 32 (two radix-32 stages); of axes of 243, 270,
+    360, 384, 400 points: the balanced plan or the two-stage one (2)
+                                                               -> e_x, e_y, e_z
   * the tile shape (lines per CTA) of every pass kind          -> r2c, c2r,
                                                                   c2c_x, c2c_y,
                                                                   c2c_z, xy_fused
@@ -80,8 +82,9 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     s = eng.empty_spectral()
     y = eng.empty_physical()
     opts = {}
+    balanced = {243: 9, 270: 30, 360: 30, 384: 24, 400: 20}  # points of the balanced plans
     for axis, n in ((0, nx), (1, ny), (2, nz)):
-        opts[axis] = [16, 32] if n in (512, 1024) else [None]
+        opts[axis] = [16, 32] if n in (512, 1024) else ([balanced[n], 2] if n in balanced else [None])
     eng.set_fusion(False)
     best = None
     for ex, ey, ez in itertools.product(opts[0], opts[1], opts[2]):
@@ -103,7 +106,8 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
             # launch forms exist for the compile-time power-of-two kernels
             # (the pipelined one in FP32 only)
             axis = {"c2c_x": 0, "c2c_y": 1, "c2c_z": 2}.get(kind, 0 if fmt == 1 else 2)
-            if kind == "xy_fused" or not pts[axis]:
+            n = (nx, ny, nz)[axis]
+            if kind == "xy_fused" or not pts[axis] or n & (n - 1):
                 forms = [(0, (0, 0))]
             else:
                 forms = [f for f in LAUNCHES if prec == 4 or f[0] == 0]

@@ -209,14 +209,15 @@ int gbfft_engine_set_fusion(gbfft_engine_t engine, int enable);
  * kind (pipe_r2c, pipe_c2r, pipe_c2c_x, ...), the cluster launch per pass
  * kind (cl_<pass> = CTAs a cluster, cls_<pass> = 1 for the start barrier),
  * fuse=0/1, and e_x / e_y / e_z,
- * the points per thread of the x / y / z plan (16: radix 16, 16, ...;
- * 32: two radix-32 stages) for axes of 512 or 1024 points.  The tuner
+ * the points per thread of the x / y / z plan (as gbfft_engine_set_plan).  The tuner
  * (2decomp-fft_gb300/tune.py) measures the choices and writes the file. */
 int gbfft_tune_cache_path(const char* path); /* NULL = default, "" = none */
-/* Re-plan axis 0, 1 or 2 (512 or 1024 points) with 16 or 32 points per
+/* Re-plan axis 0, 1 or 2: 512 or 1024 points with 16 or 32 points per
  * thread (radix 16, 16, ... or two radix-32 stages; a contiguous line of 32
- * points a thread is one warp); resets the tile shapes.  Waits for the
- * device. */
+ * points a thread is one warp); 243, 270, 360, 384 or 400 points with the
+ * balanced plan (points = 9, 30, 30, 24, 20: 9 9 3, 15 6 3, 10 6 6, 8 8 6,
+ * 20 20) or points = 2 for the two-stage plan n = R0 R1.  Resets the tile
+ * shapes.  Waits for the device. */
 int gbfft_engine_set_plan(gbfft_engine_t engine, int axis, int points);
 /* Current fusion switch, lines per CTA per pass kind (GBFFT_PASS_KINDS
  * ints, 0 = built-in) and points per thread per axis (3 ints, 0 = the axis

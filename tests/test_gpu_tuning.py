@@ -81,6 +81,42 @@ def test_contiguous_plans_double_precision(ex):
     e.close()
 
 
+BALANCED = {243: 9, 270: 30, 360: 30, 384: 24, 400: 20}
+
+
+@pytest.mark.parametrize("prec", ["s", "d"])
+@pytest.mark.parametrize("fmt", [1, 3])
+@pytest.mark.parametrize("n", sorted(BALANCED))
+@pytest.mark.parametrize("plan", ["balanced", "two-stage"])
+def test_non_power_of_two_plans_give_the_same_transform(prec, fmt, n, plan):
+    # the balanced plan (every thread busy in every stage) and the
+    # two-stage plan n = R0 R1, on every axis (contiguous and strided)
+    import gbfft
+    shapes = [(n, 12, 10), (14, n, 6), (10, 8, n)]
+    for shape in shapes:
+        nx, ny, nz = shape
+        x = np.random.default_rng(n + fmt).standard_normal((nz, ny, nx))
+        e = gbfft.Engine(fmt, nx, ny, nz, prec=gbfft.PREC_SINGLE if prec == "s" else gbfft.PREC_DOUBLE)
+        axis = shape.index(n)
+        pts = BALANCED[n] if plan == "balanced" else 2
+        e.set_plan(axis, pts)
+        assert e.tuning()["points"][axis] == pts
+        xd = torch.from_numpy(x.astype(np.float32 if prec == "s" else np.float64)).cuda()
+        s = e.empty_spectral()
+        e.r2c(xd, s)
+        tol = 2e-6 if prec == "s" else 1e-12
+        assert rel(s.cpu().numpy(), O.fft3d_r2c(x, fmt)) <= tol, shape
+        y = e.empty_physical()
+        e.c2r(s, y)
+        assert rel(y.cpu().numpy() / (nx * ny * nz), x) <= tol, shape
+        c = x + 1j * np.random.default_rng(2).standard_normal(x.shape)
+        cd = torch.from_numpy(c.astype(np.complex64 if prec == "s" else np.complex128)).cuda()
+        o = torch.empty_like(cd)
+        e.c2c(cd, o, 1)
+        assert rel(o.cpu().numpy(), O.fft3d_c2c(c.copy(), fmt, 1)) <= tol, shape
+        e.close()
+
+
 def test_tile_shapes_give_the_same_transform():
     import gbfft
     nx, ny, nz = 256, 64, 48
