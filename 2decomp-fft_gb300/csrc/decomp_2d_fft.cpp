@@ -17,6 +17,7 @@ namespace {
 
 struct Grid {
   gbfft_engine_t eng = nullptr;
+  gbfft_dtt_t dtt = nullptr;  // opt_DTT given: the r2r transforms of the grid
   bool initialised = false;
   int format = 0, nx = 0, ny = 0, nz = 0, inplace = 0;
 };
@@ -35,6 +36,7 @@ int err(int code, const std::string& m) { return gbfft::set_error(code, m.c_str(
 
 void destroy_grid(Grid& gr) {
   if (gr.eng) gbfft_engine_destroy(gr.eng);
+  if (gr.dtt) gbfft_dtt_destroy(gr.dtt);
   gr = Grid();
 }
 
@@ -120,6 +122,14 @@ int d2d_fft_get_ngrid(void) { return (int)g.grids.size(); }
 // src/fft_common.f90:66-242 (the four init overloads and engine%init)
 int d2d_fft_init(int pencil, int nx, int ny, int nz, int igrid, int opt_inplace,
                  int opt_inplace_r2c, int opt_inplace_c2r, const int* opt_skip) {
+  return d2d_fft_init_dtt(pencil, nx, ny, nz, igrid, opt_inplace, opt_inplace_r2c, opt_inplace_c2r, opt_skip,
+                          nullptr, 0);
+}
+
+// decomp_2d_fft_engine_init with opt_DTT (src/fft_fftw3_f03.f90:230-331):
+// the engine of the grid plus, when opt_dtt is given, its r2r transforms
+int d2d_fft_init_dtt(int pencil, int nx, int ny, int nz, int igrid, int opt_inplace, int opt_inplace_r2c,
+                     int opt_inplace_c2r, const int* opt_skip, const int* opt_dtt, int n_dtt) {
   if (!g.decomp_init) return err(GBFFT_ERR_STATE, "decomp_2d_init must be called first");
   if (nx == 0 && ny == 0 && nz == 0 && igrid == 0) {  // fft_init_noarg / fft_init_arg
     nx = g.nx;
@@ -145,7 +155,16 @@ int d2d_fft_init(int pencil, int nx, int ny, int nz, int igrid, int opt_inplace,
   gbfft_engine_t eng = nullptr;
   int rc = gbfft_engine_create(pencil, nx, ny, nz, inplace, opt_skip, g.prec, GBFFT_FORM_PLAIN, &eng);
   if (rc) return rc;
+  gbfft_dtt_t dtt = nullptr;
+  if (opt_dtt) {
+    rc = gbfft_dtt_create(pencil, nx, ny, nz, opt_skip, g.prec, opt_dtt, n_dtt, &dtt);
+    if (rc) {
+      gbfft_engine_destroy(eng);
+      return rc;
+    }
+  }
   gr.eng = eng;
+  gr.dtt = dtt;
   gr.initialised = true;
   gr.format = pencil;
   gr.nx = nx;
@@ -195,6 +214,27 @@ int d2d_fft_3d_c2r(void* in_c, void* out_r) {
   const Grid* gr = cur();
   if (!gr) return err(GBFFT_ERR_STATE, "FFT library must be initialised first");
   return gbfft_exec_c2r(gr->eng, in_c, out_r, g.stream);
+}
+
+// decomp_2d_dtt_3d_r2r (src/fft_fftw3_f03.f90:1959-2023) on the current grid
+int d2d_dtt_3d_r2r(void* in, void* out, int isign) {
+  const Grid* gr = cur();
+  if (!gr) return err(GBFFT_ERR_STATE, "FFT library must be initialised first");
+  if (!gr->dtt) return err(GBFFT_ERR_STATE, "No DTT for the current engine");
+  return gbfft_exec_r2r(gr->dtt, in, out, isign, g.stream);
+}
+
+// decomp_2d_fft_get_dtt_input (src/fft_fftw3_f03.f90:629-643): the forward
+// kinds 1..8 of the current grid's r2r transforms
+int d2d_fft_get_dtt_input(int kinds[3]) {
+  const Grid* gr = cur();
+  if (!gr) return err(GBFFT_ERR_STATE, "Invalid operation");
+  if (!gr->dtt) return err(GBFFT_ERR_STATE, "No DTT for the current engine");
+  int cfg[15];
+  int rc = gbfft_dtt_get_config(gr->dtt, cfg);
+  if (rc) return rc;
+  for (int k = 0; k < 3; ++k) kinds[k] = cfg[k];
+  return GBFFT_OK;
 }
 
 int d2d_fft_finalize(void) {

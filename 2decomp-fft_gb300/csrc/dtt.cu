@@ -1,0 +1,193 @@
+// Real-to-real transforms (DCT-I..IV, DST-I..IV) along one axis, the 1D
+// passes of decomp_2d_dtt_3d_r2r (src/fft_fftw3_f03.f90:1555-1656, where
+// they are FFTW r2r plans).
+//
+// Every kind is a complex FFT of length M of an extension of the window:
+//   DCT-I   M = 2(n-1): even extension x_0..x_{n-1}, x_{n-2}..x_1;  Y_k = Re F_k
+//   DST-I   M = 2(n+1): odd extension 0, x_0..x_{n-1}, 0, -x_{n-1}..-x_0;
+//                       Y_k = -Im F_{k+1}
+//   DCT-II  M = 2n: x_0..x_{n-1}, x_{n-1}..x_0;  Y_k = Re(W^k F_k)
+//   DCT-III M = 2n: c_j x_j W^j (c_0 = 1, else 2), zero padded;  Y_k = Re F_k
+//   DCT-IV  M = 2n: x_j W^j, zero padded;  Y_k = 2 Re(e^{-i pi/(4n)} W^k F_k)
+// with W = exp(-2 pi i / (4n)), and the sine kinds from the cosine ones:
+//   DST-II(x)_k  = DCT-II((-1)^j x_j)_{n-1-k}
+//   DST-III(x)_k = (-1)^k DCT-III(x_{n-1-j})_k
+//   DST-IV(x)_k  = (-1)^k DCT-IV(x_{n-1-j})_k
+// A CTA owns L lines.  Each line's extension is built in shared memory
+// straight from the real window, transformed by the runtime-planned Stockham
+// stages (fft_pp.cuh) and reduced to the n real outputs, which go back to the
+// window's positions; with src != dst the points outside the window are
+// copied through.
+#include "fft_common.cuh"
+#include "fft_pp.cuh"
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+namespace {
+
+using namespace dev;
+
+template <typename T, bool CONTIG>
+__global__ void __launch_bounds__(kMaxThreads) dtt_pass_kernel(const __grid_constant__ DttArgs a) {
+  using C = Cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int t, line;
+  long long u, v;
+  if (CONTIG) {
+    t = threadIdx.x;
+    line = threadIdx.y;
+    u = (long long)blockIdx.x * a.L + line;
+    v = 0;
+  } else {
+    line = threadIdx.x;
+    t = threadIdx.y;
+    u = (long long)blockIdx.x * a.L + line;
+    v = blockIdx.y;
+  }
+  const bool valid = u < a.nlines;
+  const long long base = CONTIG ? u * a.sl : u + v * a.sl;
+  const T* src = reinterpret_cast<const T*>(a.src);
+  T* dst = reinterpret_cast<T*>(a.dst);
+  const int n = a.n, M = a.M, kind = a.kind, tpl = a.tpl;
+  const C* w4 = reinterpret_cast<const C*>(a.w4);
+
+  LineCtx<T, K_C2C, CONTIG> c;  // shared-memory layout and twiddles of the length-M line
+  c.tw = reinterpret_cast<const C*>(a.tw);
+  c.N = M;
+  c.L = a.L;
+  c.t = t;
+  c.tpl = tpl;
+  c.line = line;
+  const size_t e = (size_t)M * a.L;
+  C* buf0 = reinterpret_cast<C*>(smem_raw);
+  C* buf1 = buf0 + (e + (e >> 4) + 1);
+
+  auto X = [&](int j) -> T { return valid ? src[base + (long long)(a.off + j) * a.sn] : T(0); };
+
+  // the extension of the window, natural order
+#pragma unroll 1
+  for (int m = t; m < M; m += tpl) {
+    C z = cmk<C>(T(0), T(0));
+    switch (kind) {
+      case 1:
+        z.x = X(m < n ? m : M - m);
+        break;
+      case 5:
+        if (m != 0 && m != n + 1) z.x = m <= n ? X(m - 1) : -X(M - m - 1);
+        break;
+      case 2:
+      case 6: {
+        const int j = m < n ? m : 2 * n - 1 - m;
+        z.x = (kind == 6 && (j & 1)) ? -X(j) : X(j);
+        break;
+      }
+      case 3:
+      case 7:
+      case 4:
+      case 8:
+        if (m < n) {
+          const T x = (kind == 3 || kind == 4) ? X(m) : X(n - 1 - m);
+          const T s = ((kind == 3 || kind == 7) && m > 0) ? T(2) : T(1);
+          const C w = w4[m];
+          z = cmk<C>(s * x * w.x, s * x * w.y);
+        }
+        break;
+      default:
+        break;
+    }
+    buf0[c.sidx(m)] = z;
+  }
+  __syncthreads();
+
+  C* A = buf0;
+  C* B = buf1;
+  int Ns = 1;
+#pragma unroll 1
+  for (int s = 0; s < a.nst; ++s) {
+    const int R = a.radix[s];
+    if (R == 16) stage_pp<T, K_C2C, CONTIG, 16>(c, A, B, Ns);
+    else if (R == 8) stage_pp<T, K_C2C, CONTIG, 8>(c, A, B, Ns);
+    else if (R == 4) stage_pp<T, K_C2C, CONTIG, 4>(c, A, B, Ns);
+    else if (R == 2) stage_pp<T, K_C2C, CONTIG, 2>(c, A, B, Ns);
+    else if (R == 3) stage_pp<T, K_C2C, CONTIG, 3>(c, A, B, Ns);
+    else if (R == 5) stage_pp<T, K_C2C, CONTIG, 5>(c, A, B, Ns);
+    else if (R == 7) stage_pp<T, K_C2C, CONTIG, 7>(c, A, B, Ns);
+    else stage_pp_generic<T, K_C2C, CONTIG>(c, A, B, R, Ns);
+    __syncthreads();
+    C* tmp = A;
+    A = B;
+    B = tmp;
+    Ns *= R;
+  }
+
+  if (!valid) return;
+  const C c0 = cmk<C>(T(a.c0x), T(a.c0y));
+#pragma unroll 1
+  for (int k = t; k < n; k += tpl) {
+    T y;
+    switch (kind) {
+      case 1:
+        y = A[c.sidx(k)].x;
+        break;
+      case 5:
+        y = -A[c.sidx(k + 1)].y;
+        break;
+      case 2:
+      case 6: {
+        const int kk = kind == 2 ? k : n - 1 - k;
+        const C f = A[c.sidx(kk)], w = w4[kk];
+        y = w.x * f.x - w.y * f.y;
+        break;
+      }
+      case 3:
+      case 7:
+        y = A[c.sidx(k)].x;
+        if (kind == 7 && (k & 1)) y = -y;
+        break;
+      default: {  // 4, 8
+        const C f = A[c.sidx(k)], w = cmul(c0, w4[k]);
+        y = T(2) * (w.x * f.x - w.y * f.y);
+        if (kind == 8 && (k & 1)) y = -y;
+        break;
+      }
+    }
+    dst[base + (long long)(a.off + k) * a.sn] = y;
+  }
+  if (a.src != a.dst) {
+#pragma unroll 1
+    for (int j = t; j < a.naxis; j += tpl)
+      if (j < a.off || j >= a.off + n) dst[base + (long long)j * a.sn] = src[base + (long long)j * a.sn];
+  }
+}
+
+template <typename T, bool CONTIG>
+cudaError_t launch_t(const DttArgs& a, cudaStream_t stream) {
+  const size_t e = (size_t)a.M * a.L;
+  const size_t smem = 2 * (e + (e >> 4) + 1) * sizeof(Cx<T>);
+  auto kern = dtt_pass_kernel<T, CONTIG>;
+  if (smem > 48 * 1024) {
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+  }
+  const dim3 block = CONTIG ? dim3(a.tpl, a.L) : dim3(a.L, a.tpl);
+  const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
+  kern<<<grid, block, smem, stream>>>(a);
+  add_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t dtt_smem_bytes(int prec_bytes, int M, int L) {
+  const size_t e = (size_t)M * (size_t)L;
+  return 2 * (e + (e >> 4) + 1) * (size_t)(2 * prec_bytes);
+}
+
+cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream) {
+  if (a.n < 1 || a.M < 2 || a.L < 1 || a.tpl < 1 || a.L * a.tpl > kMaxThreads) return cudaErrorInvalidValue;
+  if (prec_bytes == 4) return contiguous ? launch_t<float, true>(a, stream) : launch_t<float, false>(a, stream);
+  return contiguous ? launch_t<double, true>(a, stream) : launch_t<double, false>(a, stream);
+}
+
+}  // namespace gbfft

@@ -1231,3 +1231,247 @@ int gbfft_engine_profile_read(gbfft_engine_t e, int kind, long long* launches, d
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Real-to-real transforms (decomp_2d_dtt_3d_r2r, src/fft_fftw3_f03.f90:
+// 341-471 configuration, 1555-1656 the 1D passes, 1959-2023 the 3D driver)
+// ===========================================================================
+
+namespace {
+
+constexpr unsigned kDttMagic = 0x47424454u;  // "GBDT"
+
+struct DttAxis {
+  int kind = 0, off = 0, n = 0, M = 0;
+  AxisPlan plan;        // radix stages of M
+  void* tw = nullptr;   // exp(-2 pi i m / M)
+  void* w4 = nullptr;   // exp(-2 pi i m / (4 n)), m < n
+  double c0x = 1, c0y = 0;
+};
+
+}  // namespace
+
+struct gbfft_dtt_s {
+  unsigned magic = kDttMagic;
+  int format = GBFFT_PHYSICAL_IN_X;
+  int nx = 0, ny = 0, nz = 0, prec = 8;
+  int skip[3] = {0, 0, 0};
+  int cfg[15] = {0};
+  DttAxis ax[2][3];  // [forward, backward][x, y, z]
+};
+
+namespace {
+
+bool valid_dtt(gbfft_dtt_t d) { return d != nullptr && d->magic == kDttMagic; }
+
+void release_dtt(gbfft_dtt_t d) {
+  for (auto& dir : d->ax)
+    for (DttAxis& a : dir) {
+      if (a.tw) cudaFree(a.tw);
+      if (a.w4) cudaFree(a.w4);
+      a.tw = a.w4 = nullptr;
+    }
+}
+
+// The reference's configuration: dtt_assign_default (windows),
+// dtt_invert (backward kinds); src/fft_fftw3_f03.f90:341-455.
+int dtt_config(const int* in, int nin, int* c) {
+  if (!in || nin < 3) return fail(GBFFT_ERR_INVALID, "Invalid argument");
+  for (int k = 0; k < 3; ++k)
+    if (in[k] < 1 || in[k] > 8) return fail(GBFFT_ERR_INVALID, "Invalid argument");
+  for (int k = 0; k < 15; ++k) c[k] = 0;
+  if (nin == 12) {
+    for (int k = 0; k < 12; ++k) c[k] = in[k];
+    for (int k = 0; k < 3; ++k)
+      if (c[3 + k] != c[9 + k])
+        return fail(GBFFT_ERR_INVALID, "Setup is not compatible with in-place r2r transforms");
+  } else if (nin == 3) {
+    for (int k = 0; k < 3; ++k) {
+      c[k] = in[k];
+      c[3 + k] = 1;  // ifirst
+      c[6 + k] = 1;  // ndismiss
+      if (c[k] == 1) c[6 + k] = 0;  // DCT-I
+      if (c[k] == 5) {              // DST-I
+        c[3 + k] = 2;
+        c[6 + k] = 2;
+      }
+      if (c[k] == 7) c[3 + k] = 2;  // DST-III
+      c[9 + k] = c[3 + k];
+    }
+  } else {
+    return fail(GBFFT_ERR_INVALID, "Invalid argument");
+  }
+  static const int inverse[9] = {0, 1, 3, 2, 4, 5, 7, 6, 8};
+  for (int k = 0; k < 3; ++k) c[12 + k] = inverse[c[k]];
+  return GBFFT_OK;
+}
+
+int setup_dtt_axis(DttAxis& a, int kind, int first, int ndismiss, int naxis, int prec) {
+  a.kind = kind;
+  a.off = first - 1;
+  a.n = naxis - ndismiss;
+  if (a.off < 0 || a.n < 1 || a.off + a.n > naxis || (kind == 1 && a.n < 2))
+    return fail(GBFFT_ERR_INVALID, "r2r window outside the axis");
+  a.M = kind == 1 ? 2 * (a.n - 1) : kind == 5 ? 2 * (a.n + 1) : 2 * a.n;
+  std::string why;
+  if (!factorize(a.M, a.plan, why)) return fail(GBFFT_ERR_UNSUPPORTED, "r2r extension: " + why);
+  if (dtt_smem_bytes(prec, a.M, 1) > 200 * 1024)
+    return fail(GBFFT_ERR_UNSUPPORTED, "r2r extension does not fit one shared-memory tile");
+  int rc = upload_table(&a.tw, twiddles(a.M), prec);
+  if (rc != GBFFT_OK) return rc;
+  std::vector<double> w = twiddles(4 * a.n);
+  w.resize(2 * (size_t)a.n);
+  rc = upload_table(&a.w4, w, prec);
+  if (rc != GBFFT_OK) return rc;
+  const long double pi = 3.141592653589793238462643383279502884L;
+  a.c0x = (double)cosl(pi / (4.0L * a.n));
+  a.c0y = (double)(-sinl(pi / (4.0L * a.n)));
+  return GBFFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbfft_dtt_create(int format, int nx, int ny, int nz, const int* skip, int prec, const int* dtt, int ndtt,
+                     gbfft_dtt_t* out) {
+  if (!out) return fail(GBFFT_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (format != GBFFT_PHYSICAL_IN_X && format != GBFFT_PHYSICAL_IN_Z)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for pencil");
+  if (nx <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for nx");
+  if (ny <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for ny");
+  if (nz <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for nz");
+  if (prec != GBFFT_PREC_SINGLE && prec != GBFFT_PREC_DOUBLE) return fail(GBFFT_ERR_INVALID, "bad precision");
+  gbfft_dtt_t d = new gbfft_dtt_s;
+  d->format = format;
+  d->nx = nx;
+  d->ny = ny;
+  d->nz = nz;
+  d->prec = prec;
+  for (int k = 0; k < 3; ++k) d->skip[k] = skip ? (skip[k] != 0) : 0;
+  int rc = dtt_config(dtt, ndtt, d->cfg);
+  const int lens[3] = {nx, ny, nz};
+  for (int dir = 0; dir < 2 && rc == GBFFT_OK; ++dir)
+    for (int k = 0; k < 3 && rc == GBFFT_OK; ++k) {
+      if (d->skip[k]) continue;
+      const int kind = d->cfg[dir == 0 ? k : 12 + k];
+      const int first = d->cfg[dir == 0 ? 3 + k : 9 + k];
+      rc = setup_dtt_axis(d->ax[dir][k], kind, first, d->cfg[6 + k], lens[k], prec);
+    }
+  if (rc != GBFFT_OK) {
+    const std::string msg = g_err;
+    release_dtt(d);
+    d->magic = 0;
+    delete d;
+    g_err = msg;
+    return rc;
+  }
+  g_err.clear();
+  *out = d;
+  return GBFFT_OK;
+}
+
+int gbfft_dtt_destroy(gbfft_dtt_t d) {
+  if (!d) return GBFFT_OK;
+  if (!valid_dtt(d)) return fail(GBFFT_ERR_INVALID, "not an r2r engine");
+  release_dtt(d);
+  d->magic = 0;
+  delete d;
+  return GBFFT_OK;
+}
+
+int gbfft_dtt_get_config(gbfft_dtt_t d, int* cfg) {
+  if (!valid_dtt(d) || !cfg) return fail(GBFFT_ERR_INVALID, "bad argument");
+  for (int k = 0; k < 15; ++k) cfg[k] = d->cfg[k];
+  return GBFFT_OK;
+}
+
+int gbfft_exec_r2r(gbfft_dtt_t d, void* d_in, void* d_out, int isign, void* stream) {
+  if (!valid_dtt(d)) return fail(GBFFT_ERR_INVALID, "not an r2r engine");
+  if (!d_in || !d_out) return fail(GBFFT_ERR_INVALID, "null array pointer");
+  if (isign != GBFFT_FORWARD && isign != GBFFT_BACKWARD) return fail(GBFFT_ERR_INVALID, "Invalid value");
+  const size_t bytes = (size_t)d->nx * d->ny * d->nz * d->prec;
+  if (d_in != d_out && overlap(d_in, bytes, d_out, bytes))
+    return fail(GBFFT_ERR_INVALID, "input and output partially overlap");
+  if (!aligned(d_in, d->prec) || !aligned(d_out, d->prec))
+    return fail(GBFFT_ERR_INVALID, "array not aligned to its element size");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int dir = isign == GBFFT_FORWARD ? 0 : 1;
+  const bool x_first = (d->format == GBFFT_PHYSICAL_IN_X) == (isign == GBFFT_FORWARD);
+  const int order[3] = {x_first ? 0 : 2, 1, x_first ? 2 : 0};
+  const long long nx = d->nx, ny = d->ny, nz = d->nz;
+  for (int i = 0; i < 3; ++i) {
+    const int k = order[i];
+    // the first pass in place on the input, the second into the output
+    // (the transposes at one rank), the third in place on the output
+    void* src = i == 0 ? d_in : (i == 1 ? d_in : d_out);
+    void* dst = i == 0 ? d_in : d_out;
+    if (d->skip[k]) {
+      if (src != dst) {
+        cudaError_t err = launch_copy(src, dst, bytes, st);
+        if (err != cudaSuccess) return cuda_fail(err, "copy launch");
+      }
+      continue;
+    }
+    const DttAxis& ax = d->ax[dir][k];
+    DttArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.src = src;
+    a.dst = dst;
+    a.off = ax.off;
+    a.n = ax.n;
+    a.kind = ax.kind;
+    a.M = ax.M;
+    a.nst = ax.plan.nst;
+    for (int s = 0; s < kMaxStages; ++s) a.radix[s] = s < ax.plan.nst ? ax.plan.radix[s] : 0;
+    a.tw = ax.tw;
+    a.w4 = ax.w4;
+    a.c0x = ax.c0x;
+    a.c0y = ax.c0y;
+    const bool contiguous = k == 0;
+    if (k == 0) {
+      a.sn = 1;
+      a.sl = nx;
+      a.nlines = ny * nz;
+      a.nv = 1;
+      a.naxis = (int)nx;
+    } else if (k == 1) {
+      a.sn = nx;
+      a.sl = nx * ny;
+      a.nlines = nx;
+      a.nv = (int)nz;
+      a.naxis = (int)ny;
+    } else {
+      a.sn = nx * ny;
+      a.sl = nx;
+      a.nlines = nx;
+      a.nv = (int)ny;
+      a.naxis = (int)nz;
+    }
+    if (!contiguous && a.nv > 65535) return fail(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
+    // about 8 points of the extension a thread; contiguous: 128-thread CTAs,
+    // strided: 16 neighbouring lines (64-byte row segments in FP32)
+    int tpl = (ax.M + 7) / 8;
+    if (tpl < 1) tpl = 1;
+    int L;
+    if (contiguous) {
+      if (tpl > kMaxThreads) tpl = kMaxThreads;
+      L = 128 / tpl;
+      if (L < 1) L = 1;
+    } else {
+      L = 16;
+      while (L * tpl > kMaxThreads && tpl > 16) tpl /= 2;
+      while (L > 1 && L * tpl > kMaxThreads) L /= 2;
+    }
+    while (L > 1 && dtt_smem_bytes(d->prec, ax.M, L) > 100 * 1024) --L;
+    if (a.nlines < L) L = (int)a.nlines;
+    a.L = L;
+    a.tpl = tpl;
+    cudaError_t err = launch_dtt_pass(d->prec, contiguous, a, st);
+    if (err != cudaSuccess) return cuda_fail(err, "r2r pass launch");
+  }
+  return GBFFT_OK;
+}
+
+}  // extern "C"

@@ -222,6 +222,30 @@ int engine_passes(struct ::gbfft_engine_s* e, int which, const void* in, void* o
 // (two padded buffers); the power-of-two pass needs half of it.
 size_t pass_smem_bytes(int prec_bytes, int n, int L);
 
+// One real-to-real pass along an axis (dtt.cu): the window of n points
+// starting at point `off` of every line is transformed by kind 1..8
+// (DCT-I..IV, DST-I..IV) through a complex FFT of length M.
+struct DttArgs {
+  const void* src;   // real array the window is read from
+  void* dst;         // real array it is written to (may be src)
+  long long sn;      // element stride between points of a line
+  long long sl;      // contiguous: line stride; strided: stride of v
+  long long nlines;  // contiguous: lines; strided: extent of u (x positions)
+  int nv;            // strided: extent of v (grid.y)
+  int naxis;         // points on the axis (copied through outside the window)
+  int off, n;        // window: first point, length
+  int kind;          // 1..8
+  int M;             // FFT length of the extension
+  int nst;           // radix stages of M
+  int radix[kMaxStages];
+  const void* tw;    // exp(-2 pi i m / M), m < M
+  const void* w4;    // exp(-2 pi i m / (4 n)), m < n
+  double c0x, c0y;   // exp(-i pi / (4 n))
+  int L, tpl;        // lines a CTA, threads a line
+};
+size_t dtt_smem_bytes(int prec_bytes, int M, int L);
+cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream);
+
 // Enqueue one axis pass.  prec_bytes = 4 (float) or 8 (double).
 cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous,
                              const PassArgs& a, cudaStream_t stream);

@@ -67,6 +67,10 @@ SIGNATURES = {
     "gbfft_engine_set_pipeline": (_i, [_vp, _i, _i]),
     "gbfft_engine_get_pipeline": (_i, [_vp, _ip]),
     "gbfft_engine_set_cluster": (_i, [_vp, _i, _i, _i]),
+    "gbfft_dtt_create": (_i, [_i, _i, _i, _i, _ip, _i, _ip, _i, ctypes.POINTER(_vp)]),
+    "gbfft_dtt_destroy": (_i, [_vp]),
+    "gbfft_dtt_get_config": (_i, [_vp, _ip]),
+    "gbfft_exec_r2r": (_i, [_vp, _vp, _vp, _i, _vp]),
     "gbfft_engine_get_cluster": (_i, [_vp, _ip, _ip]),
     "gbfft_engine_set_fusion": (_i, [_vp, _i]),
     "gbfft_engine_status": (_i, [_vp]),
@@ -89,6 +93,9 @@ SIGNATURES = {
     "d2d_transpose_y_to_x": (_i, [_vp, _vp, _i]),
     "d2d_fft_set_default_inplace": (_i, [_i]),
     "d2d_fft_init": (_i, [_i, _i, _i, _i, _i, _i, _i, _i, _ip]),
+    "d2d_fft_init_dtt": (_i, [_i, _i, _i, _i, _i, _i, _i, _i, _ip, _ip, _i]),
+    "d2d_dtt_3d_r2r": (_i, [_vp, _vp, _i]),
+    "d2d_fft_get_dtt_input": (_i, [_ip]),
     "d2d_fft_set_ngrid": (_i, [_i]),
     "d2d_fft_get_ngrid": (_i, []),
     "d2d_fft_use_grid": (_i, [_i]),
@@ -172,6 +179,40 @@ def spectral_shape(nx, ny, nz, fmt):
     if fmt == PHYSICAL_IN_X:
         return (nz, ny, nx // 2 + 1)
     return (nz // 2 + 1, ny, nx)
+
+
+class Dtt:
+    """Real-to-real (DCT / DST) transforms of one grid (gbfft_dtt_create):
+    dtt = 3 kinds 1..8 (x, y, z) or the 12-int form with the windows."""
+
+    def __init__(self, fmt, nx, ny, nz, dtt, skip=None, prec=PREC_DOUBLE):
+        self.h = ctypes.c_void_p()
+        sk = _int3([int(bool(s)) for s in skip]) if skip is not None else None
+        arr = (ctypes.c_int * len(dtt))(*[int(v) for v in dtt])
+        check(lib().gbfft_dtt_create(int(fmt), int(nx), int(ny), int(nz), sk, int(prec), arr, len(dtt),
+                                     ctypes.byref(self.h)))
+        self.fmt, self.nx, self.ny, self.nz, self.prec = fmt, nx, ny, nz, prec
+
+    def close(self):
+        if self.h:
+            check(lib().gbfft_dtt_destroy(self.h))
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def config(self):
+        c = (ctypes.c_int * 15)()
+        check(lib().gbfft_dtt_get_config(self.h, c))
+        return list(c)
+
+    def r2r(self, x, out, isign, stream=None):
+        """decomp_2d_dtt_3d_r2r: x is modified by the first pass."""
+        check(lib().gbfft_exec_r2r(self.h, _ptr(x), _ptr(out), int(isign), _stream(stream)))
+        return out
 
 
 class Engine:
@@ -403,11 +444,26 @@ def transpose_y_to_x(src, dst, is_complex=False):
 
 
 def decomp_2d_fft_init(pencil=PHYSICAL_IN_X, nx=0, ny=0, nz=0, igrid=0, opt_inplace=None,
-                       opt_inplace_r2c=None, opt_inplace_c2r=None, opt_skip_XYZ_c2c=None):
+                       opt_inplace_r2c=None, opt_inplace_c2r=None, opt_skip_XYZ_c2c=None, opt_DTT=None):
     sk = _int3([int(bool(s)) for s in opt_skip_XYZ_c2c]) if opt_skip_XYZ_c2c is not None else None
     opt = lambda v: -1 if v is None else int(bool(v))
-    check(lib().d2d_fft_init(pencil, nx, ny, nz, igrid, opt(opt_inplace), opt(opt_inplace_r2c),
-                             opt(opt_inplace_c2r), sk))
+    if opt_DTT is None:
+        check(lib().d2d_fft_init(pencil, nx, ny, nz, igrid, opt(opt_inplace), opt(opt_inplace_r2c),
+                                 opt(opt_inplace_c2r), sk))
+    else:
+        dtt = (ctypes.c_int * len(opt_DTT))(*[int(v) for v in opt_DTT])
+        check(lib().d2d_fft_init_dtt(pencil, nx, ny, nz, igrid, opt(opt_inplace), opt(opt_inplace_r2c),
+                                     opt(opt_inplace_c2r), sk, dtt, len(opt_DTT)))
+
+
+def decomp_2d_dtt_3d_r2r(x, out, isign):
+    check(lib().d2d_dtt_3d_r2r(_ptr(x), _ptr(out), int(isign)))
+
+
+def decomp_2d_fft_get_dtt_input():
+    k = (ctypes.c_int * 3)()
+    check(lib().d2d_fft_get_dtt_input(k))
+    return tuple(k)
 
 
 def decomp_2d_fft_set_ngrid(n):

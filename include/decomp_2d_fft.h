@@ -55,6 +55,18 @@ int d2d_fft_set_default_inplace(int inplace);
  * opt_skip: NULL or three flags (opt_skip_XYZ_c2c). */
 int d2d_fft_init(int pencil, int nx, int ny, int nz, int igrid, int opt_inplace,
                  int opt_inplace_r2c, int opt_inplace_c2r, const int* opt_skip);
+/* decomp_2d_fft_init with opt_DTT (src/fft_fftw3_f03.f90:230-331, the FFTW
+ * backend's r2r option): as d2d_fft_init, plus the grid's real-to-real
+ * transforms when opt_dtt is not NULL (3 kinds or the 12-int form of
+ * gbfft_dtt_create; n_dtt its length). */
+int d2d_fft_init_dtt(int pencil, int nx, int ny, int nz, int igrid, int opt_inplace, int opt_inplace_r2c,
+                     int opt_inplace_c2r, const int* opt_skip, const int* opt_dtt, int n_dtt);
+/* decomp_2d_dtt_3d_r2r(in, out, isign) on the current grid
+ * (src/fft_fftw3_f03.f90:1959-2023); "No DTT for the current engine" when
+ * the grid was initialised without opt_DTT. */
+int d2d_dtt_3d_r2r(void* in, void* out, int isign);
+/* decomp_2d_fft_get_dtt_input (src/fft_fftw3_f03.f90:629-643). */
+int d2d_fft_get_dtt_input(int kinds[3]);
 /* decomp_2d_fft_set_ngrid / get_ngrid / use_grid (src/fft_common.f90:381-443);
  * igrid = 0 means "absent" for use_grid. */
 int d2d_fft_set_ngrid(int ngrid);

@@ -264,6 +264,42 @@ int gbfft_selftest_bounded_wait(int counter_value, int need, long long poll_limi
 int gbfft_version(int* major, int* minor);
 long long gbfft_launch_count(void);
 
+/* ---- real-to-real transforms (DCT / DST) ----------------------------------
+ * decomp_2d_dtt_3d_r2r and the opt_DTT configuration of decomp_2d_fft_init
+ * (src/fft_fftw3_f03.f90:341-471 configuration, 1555-1656 the 1D passes,
+ * 1959-2023 the 3D driver; the reference runs them as FFTW r2r plans in its
+ * FFTW backend only).  Kinds per axis, FFTW's unnormalised definitions: */
+#define GBFFT_DCT1 1 /* REDFT00 */
+#define GBFFT_DCT2 2 /* REDFT10 */
+#define GBFFT_DCT3 3 /* REDFT01 */
+#define GBFFT_DCT4 4 /* REDFT11 */
+#define GBFFT_DST1 5 /* RODFT00 */
+#define GBFFT_DST2 6 /* RODFT10 */
+#define GBFFT_DST3 7 /* RODFT01 */
+#define GBFFT_DST4 8 /* RODFT11 */
+typedef struct gbfft_dtt_s* gbfft_dtt_t;
+/* dtt: 3 kinds (x, y, z; the reference's default windows) or 12 ints: kinds,
+ * ifirst (1-based first point of the window), ndismiss (points left out),
+ * ofirst (must equal ifirst) per axis.  A window of n = n_axis - ndismiss
+ * points starting at ifirst is transformed; the other points pass through.
+ * skip: NULL or three flags (the c2c skip flags skip r2r passes too).
+ * Errors as the reference's: "Invalid argument", "Setup is not compatible
+ * with in-place r2r transforms". */
+int gbfft_dtt_create(int format, int nx, int ny, int nz, const int* skip, int prec, const int* dtt, int ndtt,
+                     gbfft_dtt_t* dtt_out);
+int gbfft_dtt_destroy(gbfft_dtt_t dtt);
+/* The 15-int configuration: forward kinds, ifirst, ndismiss, ofirst,
+ * backward kinds (inverse of DCT-II is DCT-III, of DST-II DST-III, the others
+ * their own), kinds numbered 1..8. */
+int gbfft_dtt_get_config(gbfft_dtt_t dtt, int* cfg15);
+/* decomp_2d_dtt_3d_r2r(in, out, isign): x, y, z for PHYSICAL_IN_X forward
+ * and PHYSICAL_IN_Z backward, z, y, x otherwise.  The first pass works in
+ * place on d_in (as the reference's), the result is in d_out (d_in == d_out
+ * allowed).  Unnormalised: a round trip multiplies by the product over the
+ * axes of 2(n-1) (DCT-I), 2(n+1) (DST-I) or 2n (the others), n the window
+ * length. */
+int gbfft_exec_r2r(gbfft_dtt_t dtt, void* d_in, void* d_out, int isign, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
