@@ -28,6 +28,14 @@ namespace {
 
 using namespace dev;
 
+// The length-M line's context: shared-memory layout of LineCtx, twiddles
+// from a copy of the table in shared memory.
+template <typename T, bool CONTIG>
+struct DttCtx : LineCtx<T, K_C2C, CONTIG> {
+  const Cx<T>* stw;
+  __device__ __forceinline__ Cx<T> twiddle(int e) const { return stw[e]; }
+};
+
 template <typename T, bool CONTIG>
 __global__ void __launch_bounds__(kMaxThreads) dtt_pass_kernel(const __grid_constant__ DttArgs a) {
   using C = Cx<T>;
@@ -52,7 +60,7 @@ __global__ void __launch_bounds__(kMaxThreads) dtt_pass_kernel(const __grid_cons
   const int n = a.n, M = a.M, kind = a.kind, tpl = a.tpl;
   const C* w4 = reinterpret_cast<const C*>(a.w4);
 
-  LineCtx<T, K_C2C, CONTIG> c;  // shared-memory layout and twiddles of the length-M line
+  DttCtx<T, CONTIG> c;  // shared-memory layout and twiddles of the length-M line
   c.tw = reinterpret_cast<const C*>(a.tw);
   c.N = M;
   c.L = a.L;
@@ -62,6 +70,12 @@ __global__ void __launch_bounds__(kMaxThreads) dtt_pass_kernel(const __grid_cons
   const size_t e = (size_t)M * a.L;
   C* buf0 = reinterpret_cast<C*>(smem_raw);
   C* buf1 = buf0 + (e + (e >> 4) + 1);
+  C* stw = buf1 + (e + (e >> 4) + 1);  // the M twiddles
+  c.stw = stw;
+  {
+    const int nthreads = blockDim.x * blockDim.y, tid = threadIdx.x + threadIdx.y * blockDim.x;
+    for (int m = tid; m < M; m += nthreads) stw[m] = c.tw[m];
+  }
 
   auto X = [&](int j) -> T { return valid ? src[base + (long long)(a.off + j) * a.sn] : T(0); };
 
@@ -106,14 +120,28 @@ __global__ void __launch_bounds__(kMaxThreads) dtt_pass_kernel(const __grid_cons
 #pragma unroll 1
   for (int s = 0; s < a.nst; ++s) {
     const int R = a.radix[s];
-    if (R == 16) stage_pp<T, K_C2C, CONTIG, 16>(c, A, B, Ns);
-    else if (R == 8) stage_pp<T, K_C2C, CONTIG, 8>(c, A, B, Ns);
-    else if (R == 4) stage_pp<T, K_C2C, CONTIG, 4>(c, A, B, Ns);
-    else if (R == 2) stage_pp<T, K_C2C, CONTIG, 2>(c, A, B, Ns);
-    else if (R == 3) stage_pp<T, K_C2C, CONTIG, 3>(c, A, B, Ns);
-    else if (R == 5) stage_pp<T, K_C2C, CONTIG, 5>(c, A, B, Ns);
-    else if (R == 7) stage_pp<T, K_C2C, CONTIG, 7>(c, A, B, Ns);
-    else stage_pp_generic<T, K_C2C, CONTIG>(c, A, B, R, Ns);
+    using Ctx = DttCtx<T, CONTIG>;
+    if (R == 16) stage_pp<T, K_C2C, CONTIG, 16, Ctx>(c, A, B, Ns);
+    else if (R == 8) stage_pp<T, K_C2C, CONTIG, 8, Ctx>(c, A, B, Ns);
+    else if (R == 4) stage_pp<T, K_C2C, CONTIG, 4, Ctx>(c, A, B, Ns);
+    else if (R == 2) stage_pp<T, K_C2C, CONTIG, 2, Ctx>(c, A, B, Ns);
+    else if (R == 3) stage_pp<T, K_C2C, CONTIG, 3, Ctx>(c, A, B, Ns);
+    else if (R == 5) stage_pp<T, K_C2C, CONTIG, 5, Ctx>(c, A, B, Ns);
+    else if (R == 7) stage_pp<T, K_C2C, CONTIG, 7, Ctx>(c, A, B, Ns);
+    else if (R == 11) stage_pp<T, K_C2C, CONTIG, 11, Ctx>(c, A, B, Ns);
+    else if (R == 13) stage_pp<T, K_C2C, CONTIG, 13, Ctx>(c, A, B, Ns);
+    else if (R == 17) stage_pp<T, K_C2C, CONTIG, 17, Ctx>(c, A, B, Ns);
+    else if (R == 19) stage_pp<T, K_C2C, CONTIG, 19, Ctx>(c, A, B, Ns);
+    else if (R == 23) stage_pp<T, K_C2C, CONTIG, 23, Ctx>(c, A, B, Ns);
+    else if (sizeof(T) == 4 && (R == 29 || R == 31)) {
+      // in FP64 a butterfly of 29 or 31 points does not fit the registers
+      if constexpr (sizeof(T) == 4) {
+        if (R == 29) stage_pp<T, K_C2C, CONTIG, 29, Ctx>(c, A, B, Ns);
+        else stage_pp<T, K_C2C, CONTIG, 31, Ctx>(c, A, B, Ns);
+      }
+    } else {
+      stage_pp_generic<T, K_C2C, CONTIG, Ctx>(c, A, B, R, Ns);
+    }
     __syncthreads();
     C* tmp = A;
     A = B;
@@ -163,8 +191,7 @@ __global__ void __launch_bounds__(kMaxThreads) dtt_pass_kernel(const __grid_cons
 
 template <typename T, bool CONTIG>
 cudaError_t launch_t(const DttArgs& a, cudaStream_t stream) {
-  const size_t e = (size_t)a.M * a.L;
-  const size_t smem = 2 * (e + (e >> 4) + 1) * sizeof(Cx<T>);
+  const size_t smem = dtt_smem_bytes((int)sizeof(T), a.M, a.L);
   auto kern = dtt_pass_kernel<T, CONTIG>;
   if (smem > 48 * 1024) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -181,7 +208,7 @@ cudaError_t launch_t(const DttArgs& a, cudaStream_t stream) {
 
 size_t dtt_smem_bytes(int prec_bytes, int M, int L) {
   const size_t e = (size_t)M * (size_t)L;
-  return 2 * (e + (e >> 4) + 1) * (size_t)(2 * prec_bytes);
+  return (2 * (e + (e >> 4) + 1) + (size_t)M) * (size_t)(2 * prec_bytes);  // two line buffers, twiddles
 }
 
 cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream) {

@@ -70,7 +70,20 @@ __global__ void __launch_bounds__(kMaxThreads)
     else if (R == 3) stage_pp<T, KIND, CONTIG, 3>(c, A, B, Ns);
     else if (R == 5) stage_pp<T, KIND, CONTIG, 5>(c, A, B, Ns);
     else if (R == 7) stage_pp<T, KIND, CONTIG, 7>(c, A, B, Ns);
-    else stage_pp_generic<T, KIND, CONTIG>(c, A, B, R, Ns);
+    else if (R == 11) stage_pp<T, KIND, CONTIG, 11>(c, A, B, Ns);
+    else if (R == 13) stage_pp<T, KIND, CONTIG, 13>(c, A, B, Ns);
+    else if (R == 17) stage_pp<T, KIND, CONTIG, 17>(c, A, B, Ns);
+    else if (R == 19) stage_pp<T, KIND, CONTIG, 19>(c, A, B, Ns);
+    else if (R == 23) stage_pp<T, KIND, CONTIG, 23>(c, A, B, Ns);
+    else if (sizeof(T) == 4 && (R == 29 || R == 31)) {
+      // in FP64 a butterfly of 29 or 31 points does not fit the registers
+      if constexpr (sizeof(T) == 4) {
+        if (R == 29) stage_pp<T, KIND, CONTIG, 29>(c, A, B, Ns);
+        else stage_pp<T, KIND, CONTIG, 31>(c, A, B, Ns);
+      }
+    } else {
+      stage_pp_generic<T, KIND, CONTIG>(c, A, B, R, Ns);
+    }
     __syncthreads();
     C* tmp = A;
     A = B;

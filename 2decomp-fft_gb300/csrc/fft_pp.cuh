@@ -13,9 +13,9 @@ namespace dev {
 // (0 <= b < n/R) reads points b + r n/R, multiplies by
 // W_{Ns R}^{(b mod Ns) r}, transforms, and writes points
 // (b - b mod Ns) R + b mod Ns + r Ns.  One butterfly in flight per thread.
-template <typename T, int KIND, bool CONTIG, int R>
-__device__ __forceinline__ void stage_pp(const LineCtx<T, KIND, CONTIG>& c, const Cx<T>* A, Cx<T>* B,
-                                         int Ns) {
+// Ctx: a LineCtx (or a type derived from it that supplies its own twiddle()).
+template <typename T, int KIND, bool CONTIG, int R, class Ctx = LineCtx<T, KIND, CONTIG>>
+__device__ __forceinline__ void stage_pp(const Ctx& c, const Cx<T>* A, Cx<T>* B, int Ns) {
   using C = Cx<T>;
   const int nb = c.N / R;
   const int tstride = c.N / (Ns * R);
@@ -29,7 +29,7 @@ __device__ __forceinline__ void stage_pp(const LineCtx<T, KIND, CONTIG>& c, cons
 #pragma unroll
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], c.twiddle(k * r * tstride));
     }
-    dftp<R>(v);
+    dftg<R>(v);
     const int base = (b - k) * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) B[c.sidx(base + r * Ns)] = v[r];
@@ -38,9 +38,8 @@ __device__ __forceinline__ void stage_pp(const LineCtx<T, KIND, CONTIG>& c, cons
 
 // A stage of any radix (primes above 7): each output point is a direct sum
 // over its R inputs, O(n R) per line.
-template <typename T, int KIND, bool CONTIG>
-__device__ void stage_pp_generic(const LineCtx<T, KIND, CONTIG>& c, const Cx<T>* A, Cx<T>* B, int R,
-                                 int Ns) {
+template <typename T, int KIND, bool CONTIG, class Ctx = LineCtx<T, KIND, CONTIG>>
+__device__ void stage_pp_generic(const Ctx& c, const Cx<T>* A, Cx<T>* B, int R, int Ns) {
   using C = Cx<T>;
   const int N = c.N, nb = N / R, tstride = N / (Ns * R);
 #pragma unroll 1

@@ -51,6 +51,12 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "r2c_c2r_1024x1024x512_f32_x"
 BATCH_WORKLOAD = "batched_64_grids_f32"
+# real-to-real (DCT-II on every axis, default windows: the last point of each
+# axis left out) forward + backward: name -> (nx, ny, nz, precision, kinds)
+DTT_WORKLOADS = {
+    "r2r_dct2_256x256x256_f64_x": (256, 256, 256, 8, (2, 2, 2)),
+    "r2r_dct2_256x256x256_f32_x": (256, 256, 256, 4, (2, 2, 2)),
+}
 
 
 # ---------------------------------------------------------------------------
@@ -646,9 +652,140 @@ def read_traffic(workload, kernel):
     return None
 
 
+def run_dtt(args):
+    """Real-to-real transforms: one step = decomp_2d_dtt_3d_r2r forward then
+    backward (6 axis passes, each one read and one write of the real array)."""
+    import torch
+    import numpy as np
+    import gbfft
+    from oracle import dtt as D
+    world, rank, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    nx, ny, nz, prec, kinds = DTT_WORKLOADS[args.workload]
+    rdt = torch.float32 if prec == 4 else torch.float64
+    gbfft.lib()
+    eng = gbfft.Dtt(1, nx, ny, nz, list(kinds), prec=prec)
+    rng = np.random.default_rng(7)
+    a = rng.uniform(-1, 1, (nz, ny, nx))
+    x = torch.from_numpy(a).to(rdt).to(dev)
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream(dev)
+    npts = nx * ny * nz
+
+    def step():
+        eng.r2r(x, y, -1, stream)
+        eng.r2r(y, x, 1, stream)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    l0 = gbfft.launch_count()
+    t_wall0 = time.time()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    barrier()
+    launches = gbfft.launch_count() - l0
+    clocks.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    value = sum_over_ranks(npts) / (ms * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs") or 6800.0
+    bytes_step = 6 * 2 * npts * (4 if prec == 4 else 8)
+    achieved = bytes_step / (ms * 1e-3) / 1e9
+    # end to end: input from pinned host memory, result back, every step
+    xh = torch.empty(x.shape, dtype=rdt, pin_memory=True)
+    xh.copy_(torch.from_numpy(a).to(rdt))
+    yh = torch.empty_like(xh, pin_memory=True)
+    e2e_steps = max(3, min(args.steps, 20))
+
+    def e2e_step():
+        x.copy_(xh, non_blocking=True)
+        eng.r2r(x, y, -1, stream)
+        eng.r2r(y, x, 1, stream)
+        yh.copy_(x, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps)
+    out = None
+    if rank == 0:
+        # accuracy: forward transform against the FP64 oracle, round trip
+        x.copy_(torch.from_numpy(a).to(rdt))
+        eng.r2r(x, y, -1, stream)
+        torch.cuda.synchronize()
+        cfg = D.config(kinds)
+        acc = {}
+        if not args.no_accuracy:
+            sub = (slice(0, 16), slice(None), slice(None))  # 16 z-planes of the oracle's dense matrices
+            _, ref = D.dtt_3d_r2r(a, 1, cfg, -1)
+            got = y.double().cpu().numpy()
+            acc["rel_l2_vs_fp64"] = float(np.linalg.norm((got - ref)[sub]) / np.linalg.norm(ref[sub]))
+        cpu = None
+        if not args.no_cpu:
+            t0 = time.time()
+            reps = 0
+            while time.time() - t0 < min(args.cpu_seconds, 10.0) or reps == 0:
+                D.dtt_3d_r2r(a, 1, cfg, -1)
+                reps += 1
+            dt = (time.time() - t0) / reps
+            cpu = {"value": round(npts / (2 * dt) / 1e9, 5), "unit": "GPts/s", "cores": os.cpu_count() or 1,
+                   "kind": "port",
+                   "sample": "oracle forward transform (dense float64 matrices, numpy with its BLAS threads) on "
+                             "the full grid, %d repetitions; a round trip counted as twice its time" % reps}
+        out = {
+            "metric": "3D r2r (DCT/DST) forward+backward GPts/s & %HBM roofline",
+            "value": round(value, 3), "unit": "GPts/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == 4 else "f64",
+            "data": "synthetic: seeded uniform [-1,1)",
+            "config": {"workload": "r2r DCT-II on x, y, z (default windows) forward+backward %dx%dx%d %s" % (
+                nx, ny, nz, "fp32" if prec == 4 else "fp64"), "name": args.workload, "nx": nx, "ny": ny,
+                "nz": nz, "kinds": list(kinds), "l2": "inputs larger than L2" if npts * (prec) > 130e6
+                else "inputs smaller than L2 (no flush)", "parallelism": "replicas (one grid per GPU)"},
+            "roofline": {"bound": "hbm", "kernel": "all six r2r axis passes of the step",
+                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None,
+                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(npts / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GPts/s",
+                    "ms_per_step": round(e2e_ms, 3),
+                    "h2d_bytes_per_step": x.numel() * x.element_size(),
+                    "d2h_bytes_per_step": x.numel() * x.element_size()},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(t_wall0, t_wall1),
+            "accuracy": acc,
+        }
+        print(json.dumps(out), flush=True)
+    eng.close()
+    return out
+
+
 def run_reference(args):
     world, rank, local = dist_env()
     if rank != 0:
+        return None
+    if args.workload not in WORKLOADS:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the complex-FFT workloads; "
+                          "%s has no CPU reference run" % args.workload}), flush=True)
         return None
     nx, ny, nz, fmt, prec, kind = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
@@ -682,7 +819,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [BATCH_WORKLOAD])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD] + sorted(DTT_WORKLOADS))
     ap.add_argument("--form", default="plain", choices=["plain", "split"],
                     help="plain FP32/FP64 stages, or split-FP16 tensor-core radix-16 stages (FP32 only)")
     ap.add_argument("--no-accuracy", action="store_true")
@@ -696,6 +834,8 @@ def main():
         run_reference(args)
     elif args.workload == BATCH_WORKLOAD:
         run_batched(args)
+    elif args.workload in DTT_WORKLOADS:
+        run_dtt(args)
     else:
         run_gb300(args)
 
