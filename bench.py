@@ -56,6 +56,9 @@ BATCH_WORKLOAD = "batched_64_grids_f32"
 DTT_WORKLOADS = {
     "r2r_dct2_256x256x256_f64_x": (256, 256, 256, 8, (2, 2, 2)),
     "r2r_dct2_256x256x256_f32_x": (256, 256, 256, 4, (2, 2, 2)),
+    # 257-point axes: 256-point windows, 512-point extensions
+    "r2r_dct2_257x257x257_f32_x": (257, 257, 257, 4, (2, 2, 2)),
+    "r2r_dct2_257x257x257_f64_x": (257, 257, 257, 8, (2, 2, 2)),
 }
 
 
