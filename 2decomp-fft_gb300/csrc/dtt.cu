@@ -19,6 +19,7 @@
 // window's positions; with src != dst the points outside the window are
 // copied through.
 #include "fft_common.cuh"
+#include "fft_fast.cuh"
 #include "fft_pp.cuh"
 #include "gbfft_internal.h"
 
@@ -27,6 +28,75 @@ namespace gbfft {
 namespace {
 
 using namespace dev;
+
+// Point m of the length-M extension of the window (x(j): window point j).
+template <typename C, class XF>
+__device__ __forceinline__ C extension(int kind, int m, int n, int M, const XF& X, const C* w4) {
+  using T = decltype(C::x);
+  C z = cmk<C>(T(0), T(0));
+  switch (kind) {
+    case 1:
+      z.x = X(m < n ? m : M - m);
+      break;
+    case 5:
+      if (m != 0 && m != n + 1) z.x = m <= n ? X(m - 1) : -X(M - m - 1);
+      break;
+    case 2:
+    case 6: {
+      const int j = m < n ? m : 2 * n - 1 - m;
+      z.x = (kind == 6 && (j & 1)) ? -X(j) : X(j);
+      break;
+    }
+    case 3:
+    case 7:
+    case 4:
+    case 8:
+      if (m < n) {
+        const T x = (kind == 3 || kind == 4) ? X(m) : X(n - 1 - m);
+        const T s = ((kind == 3 || kind == 7) && m > 0) ? T(2) : T(1);
+        const C w = w4[m];
+        z = cmk<C>(s * x * w.x, s * x * w.y);
+      }
+      break;
+    default:
+      break;
+  }
+  return z;
+}
+
+// Output k of the transform from the FFT F of the extension (F(i): point i).
+template <typename C, class FF>
+__device__ __forceinline__ decltype(C::x) output(int kind, int k, int n, const FF& F, const C* w4, C c0) {
+  using T = decltype(C::x);
+  T y;
+  switch (kind) {
+    case 1:
+      y = F(k).x;
+      break;
+    case 5:
+      y = -F(k + 1).y;
+      break;
+    case 2:
+    case 6: {
+      const int kk = kind == 2 ? k : n - 1 - k;
+      const C f = F(kk), w = w4[kk];
+      y = w.x * f.x - w.y * f.y;
+      break;
+    }
+    case 3:
+    case 7:
+      y = F(k).x;
+      if (kind == 7 && (k & 1)) y = -y;
+      break;
+    default: {  // 4, 8
+      const C f = F(k), w = cmul(c0, w4[k]);
+      y = T(2) * (w.x * f.x - w.y * f.y);
+      if (kind == 8 && (k & 1)) y = -y;
+      break;
+    }
+  }
+  return y;
+}
 
 // The length-M line's context: shared-memory layout of LineCtx, twiddles
 // from a copy of the table in shared memory.
@@ -81,37 +151,7 @@ __global__ void __launch_bounds__(kMaxThreads) dtt_pass_kernel(const __grid_cons
 
   // the extension of the window, natural order
 #pragma unroll 1
-  for (int m = t; m < M; m += tpl) {
-    C z = cmk<C>(T(0), T(0));
-    switch (kind) {
-      case 1:
-        z.x = X(m < n ? m : M - m);
-        break;
-      case 5:
-        if (m != 0 && m != n + 1) z.x = m <= n ? X(m - 1) : -X(M - m - 1);
-        break;
-      case 2:
-      case 6: {
-        const int j = m < n ? m : 2 * n - 1 - m;
-        z.x = (kind == 6 && (j & 1)) ? -X(j) : X(j);
-        break;
-      }
-      case 3:
-      case 7:
-      case 4:
-      case 8:
-        if (m < n) {
-          const T x = (kind == 3 || kind == 4) ? X(m) : X(n - 1 - m);
-          const T s = ((kind == 3 || kind == 7) && m > 0) ? T(2) : T(1);
-          const C w = w4[m];
-          z = cmk<C>(s * x * w.x, s * x * w.y);
-        }
-        break;
-      default:
-        break;
-    }
-    buf0[c.sidx(m)] = z;
-  }
+  for (int m = t; m < M; m += tpl) buf0[c.sidx(m)] = extension<C>(kind, m, n, M, X, w4);
   __syncthreads();
 
   C* A = buf0;
@@ -152,40 +192,98 @@ __global__ void __launch_bounds__(kMaxThreads) dtt_pass_kernel(const __grid_cons
   if (!valid) return;
   const C c0 = cmk<C>(T(a.c0x), T(a.c0y));
 #pragma unroll 1
-  for (int k = t; k < n; k += tpl) {
-    T y;
-    switch (kind) {
-      case 1:
-        y = A[c.sidx(k)].x;
-        break;
-      case 5:
-        y = -A[c.sidx(k + 1)].y;
-        break;
-      case 2:
-      case 6: {
-        const int kk = kind == 2 ? k : n - 1 - k;
-        const C f = A[c.sidx(kk)], w = w4[kk];
-        y = w.x * f.x - w.y * f.y;
-        break;
-      }
-      case 3:
-      case 7:
-        y = A[c.sidx(k)].x;
-        if (kind == 7 && (k & 1)) y = -y;
-        break;
-      default: {  // 4, 8
-        const C f = A[c.sidx(k)], w = cmul(c0, w4[k]);
-        y = T(2) * (w.x * f.x - w.y * f.y);
-        if (kind == 8 && (k & 1)) y = -y;
-        break;
-      }
-    }
-    dst[base + (long long)(a.off + k) * a.sn] = y;
-  }
+  for (int k = t; k < n; k += tpl)
+    dst[base + (long long)(a.off + k) * a.sn] = output<C>(kind, k, n, [&](int i) { return A[c.sidx(i)]; }, w4, c0);
   if (a.src != a.dst) {
 #pragma unroll 1
     for (int j = t; j < a.naxis; j += tpl)
       if (j < a.off || j >= a.off + n) dst[base + (long long)j * a.sn] = src[base + (long long)j * a.sn];
+  }
+}
+
+// Power-of-two extension length: the extension is transformed by the
+// compile-time 16-point plan (fft_fast.cuh), reading it from and leaving its
+// transform in one padded shared buffer.
+template <typename T, bool CONTIG, int M>
+__global__ void __launch_bounds__(fast_max_threads(16, sizeof(T)), 1)
+    dtt_fast_kernel(const __grid_constant__ DttArgs a) {
+  using C = Cx<T>;
+  using P = fast::P2Plan<M, 16>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* Sm = reinterpret_cast<C*>(smem_raw);
+  int t, line;
+  long long u, v;
+  if (CONTIG) {
+    t = threadIdx.x;
+    line = threadIdx.y;
+    u = (long long)blockIdx.x * a.L + line;
+    v = 0;
+  } else {
+    line = threadIdx.x;
+    t = threadIdx.y;
+    u = (long long)blockIdx.x * a.L + line;
+    v = blockIdx.y;
+  }
+  const bool valid = u < a.nlines;
+  const long long base = CONTIG ? u * a.sl : u + v * a.sl;
+  const T* src = reinterpret_cast<const T*>(a.src);
+  T* dst = reinterpret_cast<T*>(a.dst);
+  const int n = a.n, kind = a.kind;
+  const C* w4 = reinterpret_cast<const C*>(a.w4);
+  LineCtx<T, K_C2C, CONTIG> c;
+  c.tw = reinterpret_cast<const C*>(a.twf);
+  c.N = M;
+  c.L = a.L;
+  c.t = t;
+  c.tpl = P::TPL;
+  c.line = line;
+  c.inverse = false;
+  auto X = [&](int j) -> T { return valid ? src[base + (long long)(a.off + j) * a.sn] : T(0); };
+#pragma unroll 1
+  for (int m = t; m < M; m += P::TPL) Sm[c.sidx(m)] = extension<C>(kind, m, n, M, X, w4);
+  __syncthreads();
+  C x[16];
+  fast::run_plan<P, 0, LineCtx<T, K_C2C, CONTIG>, C, true, true>(c, Sm, x);
+  if (!valid) return;
+  const C c0 = cmk<C>(T(a.c0x), T(a.c0y));
+#pragma unroll 1
+  for (int k = t; k < n; k += P::TPL)
+    dst[base + (long long)(a.off + k) * a.sn] = output<C>(kind, k, n, [&](int i) { return Sm[c.sidx(i)]; }, w4, c0);
+  if (a.src != a.dst) {
+#pragma unroll 1
+    for (int j = t; j < a.naxis; j += P::TPL)
+      if (j < a.off || j >= a.off + n) dst[base + (long long)j * a.sn] = src[base + (long long)j * a.sn];
+  }
+}
+
+template <typename T, bool CONTIG, int M>
+cudaError_t launch_fast_m(const DttArgs& a, cudaStream_t stream) {
+  constexpr int TPL = M / 16;
+  if (a.tpl != TPL || a.L * TPL > fast_max_threads(16, (int)sizeof(T))) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)fast_smem_entries(M, a.L) * sizeof(Cx<T>);
+  auto kern = dtt_fast_kernel<T, CONTIG, M>;
+  if (smem > 48 * 1024) {
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+  }
+  const dim3 block = CONTIG ? dim3(TPL, a.L) : dim3(a.L, TPL);
+  const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
+  kern<<<grid, block, smem, stream>>>(a);
+  add_launches(1);
+  return cudaGetLastError();
+}
+
+template <typename T, bool CONTIG>
+cudaError_t launch_fast(const DttArgs& a, cudaStream_t s) {
+  switch (a.M) {
+    case 32: return launch_fast_m<T, CONTIG, 32>(a, s);
+    case 64: return launch_fast_m<T, CONTIG, 64>(a, s);
+    case 128: return launch_fast_m<T, CONTIG, 128>(a, s);
+    case 256: return launch_fast_m<T, CONTIG, 256>(a, s);
+    case 512: return launch_fast_m<T, CONTIG, 512>(a, s);
+    case 1024: return launch_fast_m<T, CONTIG, 1024>(a, s);
+    case 2048: return launch_fast_m<T, CONTIG, 2048>(a, s);
+    default: return cudaErrorNotSupported;
   }
 }
 
@@ -212,7 +310,13 @@ size_t dtt_smem_bytes(int prec_bytes, int M, int L) {
 }
 
 cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream) {
-  if (a.n < 1 || a.M < 2 || a.L < 1 || a.tpl < 1 || a.L * a.tpl > kMaxThreads) return cudaErrorInvalidValue;
+  if (a.n < 1 || a.M < 2 || a.L < 1 || a.tpl < 1) return cudaErrorInvalidValue;
+  if (a.twf) {
+    if (!dtt_fast_length(a.M)) return cudaErrorInvalidValue;
+    if (prec_bytes == 4) return contiguous ? launch_fast<float, true>(a, stream) : launch_fast<float, false>(a, stream);
+    return contiguous ? launch_fast<double, true>(a, stream) : launch_fast<double, false>(a, stream);
+  }
+  if (a.L * a.tpl > kMaxThreads) return cudaErrorInvalidValue;
   if (prec_bytes == 4) return contiguous ? launch_t<float, true>(a, stream) : launch_t<float, false>(a, stream);
   return contiguous ? launch_t<double, true>(a, stream) : launch_t<double, false>(a, stream);
 }

@@ -1245,6 +1245,7 @@ struct DttAxis {
   int kind = 0, off = 0, n = 0, M = 0;
   AxisPlan plan;        // radix stages of M
   void* tw = nullptr;   // exp(-2 pi i m / M)
+  void* twf = nullptr;  // power-of-two M: stage-major table of the 16-point plan
   void* w4 = nullptr;   // exp(-2 pi i m / (4 n)), m < n
   double c0x = 1, c0y = 0;
 };
@@ -1268,8 +1269,9 @@ void release_dtt(gbfft_dtt_t d) {
   for (auto& dir : d->ax)
     for (DttAxis& a : dir) {
       if (a.tw) cudaFree(a.tw);
+      if (a.twf) cudaFree(a.twf);
       if (a.w4) cudaFree(a.w4);
-      a.tw = a.w4 = nullptr;
+      a.tw = a.twf = a.w4 = nullptr;
     }
 }
 
@@ -1319,6 +1321,12 @@ int setup_dtt_axis(DttAxis& a, int kind, int first, int ndismiss, int naxis, int
     return fail(GBFFT_ERR_UNSUPPORTED, "r2r extension does not fit one shared-memory tile");
   int rc = upload_table(&a.tw, twiddles(a.M), prec);
   if (rc != GBFFT_OK) return rc;
+  if (dtt_fast_length(a.M)) {
+    std::vector<int> radices;
+    for (int s = 0; s < fast_nst(a.M, 16); ++s) radices.push_back(fast_radix(a.M, 16, s));
+    rc = upload_table(&a.twf, stage_twiddles(radices), prec);
+    if (rc != GBFFT_OK) return rc;
+  }
   std::vector<double> w = twiddles(4 * a.n);
   w.resize(2 * (size_t)a.n);
   rc = upload_table(&a.w4, w, prec);
@@ -1426,6 +1434,7 @@ int gbfft_exec_r2r(gbfft_dtt_t d, void* d_in, void* d_out, int isign, void* stre
     a.nst = ax.plan.nst;
     for (int s = 0; s < kMaxStages; ++s) a.radix[s] = s < ax.plan.nst ? ax.plan.radix[s] : 0;
     a.tw = ax.tw;
+    a.twf = ax.twf;
     a.w4 = ax.w4;
     a.c0x = ax.c0x;
     a.c0y = ax.c0y;
@@ -1450,6 +1459,20 @@ int gbfft_exec_r2r(gbfft_dtt_t d, void* d_in, void* d_out, int isign, void* stre
       a.naxis = (int)nz;
     }
     if (!contiguous && a.nv > 65535) return fail(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
+    if (ax.twf) {
+      // compile-time 16-point plan: M / 16 threads a line; contiguous
+      // 128-thread CTAs, strided up to 16 neighbouring lines
+      const int tplf = ax.M / 16, maxt = fast_max_threads(16, d->prec);
+      int Lf = contiguous ? (tplf >= 128 ? 1 : 128 / tplf) : 16;
+      while (Lf > 1 && Lf * tplf > maxt) --Lf;
+      while (Lf > 1 && (size_t)fast_smem_entries(ax.M, Lf) * 2 * d->prec > 100 * 1024) --Lf;
+      if (a.nlines < Lf) Lf = (int)a.nlines;
+      a.L = Lf;
+      a.tpl = tplf;
+      cudaError_t err = launch_dtt_pass(d->prec, contiguous, a, st);
+      if (err != cudaSuccess) return cuda_fail(err, "r2r pass launch");
+      continue;
+    }
     // about 8 points of the extension a thread; contiguous: 128-thread CTAs,
     // strided: 16 neighbouring lines (64-byte row segments in FP32)
     int tpl = (ax.M + 7) / 8;

@@ -54,8 +54,10 @@ template <bool WARP_LOCAL> __device__ __forceinline__ void stage_barrier() {
 // global memory.
 // A compile-time plan P (P2Plan, GenPlan): line length P::N, P::E points a
 // thread, P::TPL threads a line, P::NST stages of radix P::radix(s) after
-// P::ns(s) points; every radix divides E.
-template <class P, int S, class Ctx, class C, bool SMEM0 = false>
+// P::ns(s) points; every radix divides E.  TO_SMEM: the last stage writes
+// its outputs to Sm in natural order (slot sidx) and synchronises instead of
+// storing them to global memory.
+template <class P, int S, class Ctx, class C, bool SMEM0 = false, bool TO_SMEM = false>
 __device__ __forceinline__ void run_plan(const Ctx& c, C* Sm, C (&v)[P::E]) {
   constexpr int N = P::N, E = P::E;
   constexpr int KIND = Ctx::kind;
@@ -106,7 +108,7 @@ __device__ __forceinline__ void run_plan(const Ctx& c, C* Sm, C (&v)[P::E]) {
       }
       dftg<R>(&v[m * R]);
     }
-    if constexpr (LAST && KIND != K_R2C) {
+    if constexpr (LAST && KIND != K_R2C && !TO_SMEM) {
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         const int b = t + m * TPL;
@@ -138,7 +140,7 @@ __device__ __forceinline__ void run_plan(const Ctx& c, C* Sm, C (&v)[P::E]) {
       if constexpr (LAST) __syncthreads();
       else stage_barrier<WL>();
     }
-    run_plan<P, S + 1, Ctx, C, SMEM0>(c, Sm, v);
+    run_plan<P, S + 1, Ctx, C, SMEM0, TO_SMEM>(c, Sm, v);
   }
 }
 

@@ -239,11 +239,15 @@ struct DttArgs {
   int nst;           // radix stages of M
   int radix[kMaxStages];
   const void* tw;    // exp(-2 pi i m / M), m < M
+  const void* twf;   // power-of-two M: stage-major table of the 16-point plan,
+                     // which runs instead of the runtime plan (null: runtime plan)
   const void* w4;    // exp(-2 pi i m / (4 n)), m < n
   double c0x, c0y;   // exp(-i pi / (4 n))
   int L, tpl;        // lines a CTA, threads a line
 };
 size_t dtt_smem_bytes(int prec_bytes, int M, int L);
+// power-of-two extension lengths with a compile-time plan for the r2r pass
+__host__ __device__ constexpr bool dtt_fast_length(int M) { return M >= 32 && M <= 2048 && (M & (M - 1)) == 0; }
 cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream);
 
 // Enqueue one axis pass.  prec_bytes = 4 (float) or 8 (double).

@@ -143,3 +143,51 @@ def test_module_api_opt_dtt():
         G.decomp_2d_fft_finalize()
     finally:
         G.decomp_2d_finalize()
+
+
+# Axes of 2^k + 1 points: every kind's default window has a power-of-two
+# extension (DCT-I 2^k + 1 points -> 2^(k+1); DST-I 2^k - 1 -> 2^(k+1); the
+# others 2^k -> 2^(k+1)), which runs the compile-time plan.
+@pytest.mark.parametrize("prec", [8, 4])
+@pytest.mark.parametrize("fmt", [1, 3])
+@pytest.mark.parametrize("shape", [(17, 33, 65), (129, 9, 17), (1025, 5, 3)])
+def test_r2r_power_of_two_extensions_against_oracle(prec, fmt, shape):
+    import gbfft
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx + ny + nz + fmt)
+    for k in range(1, 9):
+        kinds = [k, k, k]
+        a = rng.standard_normal((nz, ny, nx))
+        cfg = D.config(kinds)
+        e = gbfft.Dtt(fmt, nx, ny, nz, kinds, prec=prec)
+        for isign in (-1, 1):
+            x = torch.from_numpy(a).to(dtype(prec)).cuda()
+            out = torch.empty_like(x)
+            e.r2r(x, out, isign)
+            _, ref = D.dtt_3d_r2r(a, fmt, cfg, isign)
+            assert rel(out.cpu().numpy(), ref) <= TOL[prec], (k, isign)
+        e.close()
+
+
+@pytest.mark.parametrize("fmt", [1, 3])
+def test_round_trip_all_512_combinations_power_of_two_extensions(fmt):
+    import gbfft
+    nx, ny, nz = 17, 33, 9
+    ii = np.arange(1, nx + 1) / nx
+    jj = np.arange(1, ny + 1) / ny
+    kk = np.arange(1, nz + 1) / nz
+    a0 = kk[:, None, None] * jj[None, :, None] * ii[None, None, :]
+    eps = np.finfo(np.float64).eps
+    for kinds in itertools.product(range(1, 9), repeat=3):
+        e = gbfft.Dtt(fmt, nx, ny, nz, list(kinds), prec=8)
+        cfg = e.config()
+        x = torch.from_numpy(a0).cuda()
+        out = torch.zeros_like(x)
+        e.r2r(x, out, -1)
+        e.r2r(out, x, 1)
+        back = x.cpu().numpy() / D.roundtrip_scale(cfg, (nx, ny, nz))
+        sl = []
+        for d, n in ((2, nz), (1, ny), (0, nx)):
+            sl.append(slice(cfg[3 + d] - 1, n - cfg[6 + d] + cfg[3 + d] - 1))
+        assert np.abs(back - a0)[tuple(sl)].max() <= 100 * eps, kinds
+        e.close()
