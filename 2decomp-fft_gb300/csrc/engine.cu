@@ -204,6 +204,7 @@ struct TuneEntry {
   int csize[GBFFT_PASS_KINDS] = {0};
   int csync[GBFFT_PASS_KINDS] = {0};
   int e[3] = {0, 0, 0};
+  int pad = -1, flat = -1;
 };
 
 std::mutex g_tune_mu;
@@ -250,6 +251,8 @@ void load_tune_locked() {
       else if (k == "e_x") t.e[0] = v;
       else if (k == "e_y") t.e[1] = v;
       else if (k == "e_z") t.e[2] = v;
+      else if (k == "pad") t.pad = v;
+      else if (k == "flat") t.flat = v;
       for (int i = 0; i < GBFFT_PASS_KINDS; ++i) {
         if (k == names[i]) t.L[i] = v;
         if (k == std::string("pipe_") + names[i]) t.pipe[i] = v;
@@ -302,6 +305,14 @@ struct gbfft_engine_s {
   long long sync_planes = 0;
   void* work = nullptr;
   size_t work_bytes = 0;
+  // Row layout: `pad` -- the work area's rows of complex values start on
+  // kRowAlignBytes boundaries (its row pitch is sp[0] rounded up) and every
+  // r2c / c2r pass but the last writes there, so that the strided passes
+  // store whole 32-byte sectors; `flat` -- z passes whose output rows are
+  // unpadded and not so aligned take the lines of each (x, y) plane flat
+  // (segments aligned as the plane is).
+  bool pad = false;
+  bool flat = true;
 };
 
 namespace {
@@ -331,6 +342,18 @@ void release(gbfft_engine_t e) {
 }
 
 size_t cbytes(const gbfft_engine_s* e) { return 2 * (size_t)e->prec; }
+
+// Row pitch (complex elements) of the work area.
+constexpr size_t kRowAlignBytes = 64;
+long long padded_pitch(const gbfft_engine_s* e) {
+  const long long q = (long long)(kRowAlignBytes / cbytes(e));
+  return (e->sp[0] + q - 1) / q * q;
+}
+long long work_pitch(const gbfft_engine_s* e) { return e->pad ? padded_pitch(e) : e->sp[0]; }
+// Rows of n elements of `bytes` each whose tiles of 16 lines start on
+// 32-byte sectors and fill each row: taken per row, a z pass over them is
+// as aligned as a flat one.
+bool rows_aligned(long long n, size_t bytes) { return (n * (long long)bytes) % 32 == 0 && n % 16 == 0; }
 
 // Lines per CTA for a pass with the given plan.
 int lines_per_cta(const AxisPlan& p, int prec, bool contiguous, long long nlines, int* tpl_out,
@@ -487,7 +510,8 @@ void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int ki
     a.pipe = 0;
     a.csize = csize > 1 ? csize : 0;
     a.csync = a.csize ? csync : 0;
-    if (pipe > 0 && prec == 4 && pipe_length(p.n)) {
+    // (the pipelined kernel's copy loop addresses lines as (u, v) only)
+    if (pipe > 0 && prec == 4 && pipe_length(p.n) && a.row_w == 0) {
       // power-of-two tile heights only (the copy loop indexes by shifts),
       // and every buffer of the CTA within the shared-memory limit
       int L = 1;
@@ -529,9 +553,11 @@ struct Pass {
   bool fused_xfirst = true;
 };
 
-// c2c along `axis` of a complex (n1, n2, n3) array.
+// c2c along `axis` of a complex (n1, n2, n3) array whose rows of n1 values
+// lie `pin` (source) and `pout` (destination) elements apart.  A z pass
+// into unpadded rows takes each plane's lines flat when the engine says so.
 Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const void* src, void* dst,
-              int inverse) {
+              int inverse, long long pin, long long pout) {
   Pass P;
   PassArgs& a = P.a;
   std::memset(&a, 0, sizeof(a));
@@ -542,21 +568,33 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
   if (axis == 0) {
     P.contiguous = true;
     a.s_src_n = a.s_dst_n = 1;
-    a.s_src_l = a.s_dst_l = n1;
+    a.s_src_l = pin;
+    a.s_dst_l = pout;
     a.nlines = n2 * n3;
     a.nv = 1;
   } else if (axis == 1) {
     P.contiguous = false;
-    a.s_src_n = a.s_dst_n = n1;
-    a.s_src_l = a.s_dst_l = (long long)n1 * n2;
+    a.s_src_n = pin;
+    a.s_dst_n = pout;
+    a.s_src_l = pin * n2;
+    a.s_dst_l = pout * n2;
     a.nlines = n1;
     a.nv = n3;
   } else {
     P.contiguous = false;
-    a.s_src_n = a.s_dst_n = (long long)n1 * n2;
-    a.s_src_l = a.s_dst_l = n1;
+    a.s_src_n = pin * n2;
+    a.s_dst_n = pout * n2;
+    a.s_src_l = pin;
+    a.s_dst_l = pout;
     a.nlines = n1;
     a.nv = n2;
+    if (e->flat && pout == n1 && !rows_aligned(n1, cbytes(e))) {
+      a.nlines = n1 * n2;
+      a.nv = 1;
+      a.row_w = n1;
+      a.s_src_r = pin;
+      a.s_dst_r = pout;
+    }
   }
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C, e->tile_L[GBFFT_PASS_C2C_X + axis],
             e->form == GBFFT_FORM_SPLIT, e->pipe[GBFFT_PASS_C2C_X + axis], e->csize[GBFFT_PASS_C2C_X + axis],
@@ -566,8 +604,10 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
   return P;
 }
 
-// r2c (kind K_R2C) or c2r (K_C2R) along the engine's real axis.
-Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst) {
+// r2c (kind K_R2C) or c2r (K_C2R) along the engine's real axis; the
+// complex side's rows lie `cp` elements apart.  Along z into unpadded rows
+// the lines of each plane are taken flat when the engine says so.
+Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst, long long cp) {
   Pass P;
   PassArgs& a = P.a;
   std::memset(&a, 0, sizeof(a));
@@ -576,19 +616,29 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst) {
   P.kind = kind;
   const int nx = e->nx, ny = e->ny, nz = e->nz;
   long long real_s_n, real_s_l, cplx_s_n, cplx_s_l;
+  bool flat = false;
   if (e->format == GBFFT_PHYSICAL_IN_X) {
     P.contiguous = true;
     real_s_n = cplx_s_n = 1;
     real_s_l = nx;
-    cplx_s_l = nx / 2 + 1;
+    cplx_s_l = cp;
     a.real_lines = ny * nz;
     a.nv = 1;
   } else {
     P.contiguous = false;
-    real_s_n = cplx_s_n = (long long)nx * ny;
-    real_s_l = cplx_s_l = nx;
+    real_s_n = (long long)nx * ny;
+    cplx_s_n = cp * ny;
+    real_s_l = nx;
+    cplx_s_l = cp;
     a.real_lines = nx;
     a.nv = ny;
+    // the output rows: complex (pitch cp) for r2c, real (nx) for c2r
+    flat = e->flat && (kind == K_C2R ? !rows_aligned(nx, (size_t)e->prec) : (cp == nx && !rows_aligned(nx, cbytes(e))));
+    if (flat) {
+      a.real_lines = nx * ny;
+      a.nv = 1;
+      a.row_w = nx;
+    }
   }
   a.nlines = (a.real_lines + 1) / 2;
   if (kind == K_R2C) {
@@ -603,6 +653,10 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst) {
     a.s_dst_n = real_s_n;
     a.s_dst_l = real_s_l;
     a.inverse = 1;
+  }
+  if (flat) {
+    a.s_src_r = a.s_src_l;
+    a.s_dst_r = a.s_dst_l;
   }
   // strided pairs are neighbouring x positions: 8-byte aligned when nx is
   // even (every line then starts at an even real index)
@@ -718,16 +772,27 @@ namespace {
 
 // The passes of a 3D r2c (src/fft_common_3d.f90:121-189): the r2c pass
 // along the real axis into `out`, then the c2c passes on `out`.
+// With a work area, every pass but the last writes it (rows padded to
+// aligned starts) and the last one writes `out`.
 std::vector<Pass> r2c_passes(gbfft_engine_s* e, const void* d_in, void* d_out) {
   std::vector<Pass> ps;
   const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
-  ps.push_back(real_pass(e, K_R2C, d_in, d_out));
-  if (e->format == GBFFT_PHYSICAL_IN_X) {
-    if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
-    if (!e->skip[2]) ps.push_back(c2c_pass(e, 2, s1, s2, s3, d_out, d_out, 0));
-  } else {
-    if (!e->skip[1]) ps.push_back(c2c_pass(e, 1, s1, s2, s3, d_out, d_out, 0));
-    if (!e->skip[0]) ps.push_back(c2c_pass(e, 0, s1, s2, s3, d_out, d_out, 0));
+  const int order_x[2] = {1, 2}, order_z[2] = {1, 0};
+  const int* order = e->format == GBFFT_PHYSICAL_IN_X ? order_x : order_z;
+  int axes[2], na = 0;
+  for (int i = 0; i < 2; ++i)
+    if (!e->skip[order[i]]) axes[na++] = order[i];
+  void* W = e->inplace ? nullptr : e->work;
+  const long long wp = W ? work_pitch(e) : s1;
+  void* mid = W ? W : d_out;
+  ps.push_back(real_pass(e, K_R2C, d_in, na ? mid : d_out, na ? wp : s1));
+  const void* cur = na ? mid : d_out;
+  long long cp = na ? wp : s1;
+  for (int i = 0; i < na; ++i) {
+    const bool last = i == na - 1;
+    ps.push_back(c2c_pass(e, axes[i], s1, s2, s3, cur, last ? d_out : mid, 0, cp, last ? s1 : wp));
+    cur = last ? d_out : mid;
+    cp = last ? s1 : wp;
   }
   return ps;
 }
@@ -738,17 +803,20 @@ std::vector<Pass> c2r_passes(gbfft_engine_s* e, void* d_in, void* d_out) {
   std::vector<Pass> ps;
   void* W = e->inplace ? d_in : e->work;
   const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
+  const long long wp = e->inplace ? s1 : work_pitch(e);
   const void* cur = d_in;
+  long long cp = s1;
   const int order_x[2] = {2, 1};  // PHYSICAL_IN_X: z then y, then c2r along x
   const int order_z[2] = {0, 1};  // PHYSICAL_IN_Z: x then y, then c2r along z
   const int* order = e->format == GBFFT_PHYSICAL_IN_X ? order_x : order_z;
   for (int i = 0; i < 2; ++i) {
     const int ax = order[i];
     if (e->skip[ax]) continue;
-    ps.push_back(c2c_pass(e, ax, s1, s2, s3, cur, W, 1));
+    ps.push_back(c2c_pass(e, ax, s1, s2, s3, cur, W, 1, cp, wp));
     cur = W;
+    cp = wp;
   }
-  ps.push_back(real_pass(e, K_C2R, cur, d_out));
+  ps.push_back(real_pass(e, K_C2R, cur, d_out, cp));
   return ps;
 }
 
@@ -874,9 +942,10 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
       return rc;
     }
   }
-  // c2r work area: the complex intermediate, unless the input may be used
+  // work area: the complex intermediate of r2c and c2r with padded rows,
+  // unless the transforms must work in the arrays they are given
   if (!e->inplace) {
-    e->work_bytes = (size_t)e->sp[0] * e->sp[1] * e->sp[2] * cbytes(e);
+    e->work_bytes = (size_t)padded_pitch(e) * e->sp[1] * e->sp[2] * cbytes(e);
     cudaError_t err = cudaMalloc(&e->work, e->work_bytes);
     if (err != cudaSuccess) {
       e->work = nullptr;
@@ -910,6 +979,8 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
       e->csync[k] = 0;
     }
   if (tune.fuse >= 0) e->fuse = tune.fuse != 0;
+  if (tune.pad >= 0) e->pad = tune.pad != 0;
+  if (tune.flat >= 0) e->flat = tune.flat != 0;
   g_err.clear();
   *engine = e;
   return GBFFT_OK;
@@ -996,7 +1067,7 @@ int gbfft_exec_c2c(gbfft_engine_t e, void* d_in, void* d_out, int isign, void* s
   for (int i = 0; i < 3; ++i) {
     const int ax = order[i];
     if (e->skip[ax]) continue;
-    ps.push_back(c2c_pass(e, ax, n1, n2, n3, cur, d_out, inv));
+    ps.push_back(c2c_pass(e, ax, n1, n2, n3, cur, d_out, inv, n1, n1));
     cur = d_out;
   }
   if (ps.empty()) {
@@ -1201,6 +1272,20 @@ int gbfft_engine_get_tuning(gbfft_engine_t e, int* fuse, int* tiles, int* points
   if (points)
     for (int d = 0; d < 3; ++d)
       points[d] = (fast_length(e->ax[d].n) || gen_length(e->ax[d].n)) ? e->ax[d].fast_e : 0;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_set_layout(gbfft_engine_t e, int pad, int flat) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  e->pad = pad != 0;
+  e->flat = flat != 0;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_get_layout(gbfft_engine_t e, int* pad, int* flat) {
+  if (!valid_engine(e) || !pad || !flat) return fail(GBFFT_ERR_INVALID, "bad argument");
+  *pad = e->pad ? 1 : 0;
+  *flat = e->flat ? 1 : 0;
   return GBFFT_OK;
 }
 

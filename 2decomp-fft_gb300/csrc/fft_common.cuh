@@ -412,6 +412,10 @@ struct LineCtx {
       has1 = false;
       sb0 = CONTIG ? cl * a.s_src_l : cl + v * a.s_src_l;
       db0 = CONTIG ? cl * a.s_dst_l : cl + v * a.s_dst_l;
+      if (!CONTIG && a.row_w > 0) {
+        sb0 = flat_off(cl, a.row_w, a.s_src_r);
+        db0 = flat_off(cl, a.row_w, a.s_dst_r);
+      }
       sb1 = sb0;
       db1 = db0;
     } else {
@@ -421,7 +425,19 @@ struct LineCtx {
       sb1 = CONTIG ? r1 * a.s_src_l : r1 + v * a.s_src_l;
       db0 = CONTIG ? r0 * a.s_dst_l : r0 + v * a.s_dst_l;
       db1 = CONTIG ? r1 * a.s_dst_l : r1 + v * a.s_dst_l;
+      if (!CONTIG && a.row_w > 0) {
+        sb0 = flat_off(r0, a.row_w, a.s_src_r);
+        sb1 = flat_off(r1, a.row_w, a.s_src_r);
+        db0 = flat_off(r0, a.row_w, a.s_dst_r);
+        db1 = flat_off(r1, a.row_w, a.s_dst_r);
+      }
     }
+  }
+  // Start of flat line u of a plane whose rows of w lines lie `pitch`
+  // elements apart (u < 2^31: the engine bounds the lines of a plane).
+  __device__ __forceinline__ static long long flat_off(long long u, int w, long long pitch) {
+    const unsigned q = (unsigned)u / (unsigned)w;
+    return (long long)q * pitch + ((unsigned)u - q * (unsigned)w);
   }
 
   // One pad slot every 16 entries: 8-byte values are served per half-warp

@@ -68,6 +68,12 @@ struct PassArgs {
                    // reach DRAM together)
   int csync;       // with csize: the CTAs of a cluster start with a
                    // cluster barrier
+  int row_w;       // strided, nv == 1: 0, or the lines are the positions
+                   // of whole (x, y) planes taken flat: line u is point
+                   // (u % row_w, u / row_w) of the plane and starts at
+                   // u % row_w + (u / row_w) * s_src_r (s_dst_r), so that
+                   // a tile's row segments are as aligned as the plane
+  long long s_src_r, s_dst_r;
   int radix[kMaxStages];
 };
 

@@ -73,6 +73,8 @@ SIGNATURES = {
     "gbfft_exec_r2r": (_i, [_vp, _vp, _vp, _i, _vp]),
     "gbfft_engine_get_cluster": (_i, [_vp, _ip, _ip]),
     "gbfft_engine_set_fusion": (_i, [_vp, _i]),
+    "gbfft_engine_set_layout": (_i, [_vp, _i, _i]),
+    "gbfft_engine_get_layout": (_i, [_vp, _ip, _ip]),
     "gbfft_engine_status": (_i, [_vp]),
     "gbfft_tune_cache_path": (_i, [ctypes.c_char_p]),
     "gbfft_engine_set_plan": (_i, [_vp, _i, _i]),
@@ -288,6 +290,17 @@ class Engine:
         d = (ctypes.c_int * len(PASS_NAMES))()
         check(lib().gbfft_engine_get_pipeline(self.h, d))
         return dict(zip(PASS_NAMES, d))
+    def set_layout(self, pad=True, flat=True):
+        """Padded work-area rows (aligned row segments for the strided passes;
+        default off) and flat z passes over unpadded misaligned planes
+        (default on)."""
+        check(lib().gbfft_engine_set_layout(self.h, int(bool(pad)), int(bool(flat))))
+
+    def layout(self):
+        p, f = ctypes.c_int(), ctypes.c_int()
+        check(lib().gbfft_engine_get_layout(self.h, ctypes.byref(p), ctypes.byref(f)))
+        return bool(p.value), bool(f.value)
+
     def set_fusion(self, enable):
         """Fuse the x and y passes of each z-plane into one kernel (default on)."""
         check(lib().gbfft_engine_set_fusion(self.h, int(bool(enable))))

@@ -17,6 +17,7 @@ creation (tune_cache.txt beside this file, or $GBFFT_TUNE_CACHE):
     buffers                                                    -> cl_<pass>,
                                                                   cls_<pass>,
                                                                   pipe_<pass>
+  * row layout: padded work-area rows, flat z passes          -> pad, flat
   * pass fusion: x and y passes of each z-plane in one kernel  -> fuse
 
 The measured step is the benchmark's: one r2c then one c2r, per-pass device
@@ -151,6 +152,17 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     for kind, c in clusters.items():
         if c[0]:
             eng.set_cluster(kind, *c)
+    # row layout, the built-in one (unpadded rows, flat z passes over
+    # misaligned planes) unless another wins the step by 1 %
+    layout = (False, True)
+    _, step_base = measure(eng, x, s, y)
+    for lay in ((True, True), (False, False), (True, False)):
+        eng.set_layout(*lay)
+        _, st = measure(eng, x, s, y)
+        log("  layout pad=%d flat=%d: %.4f ms (built-in %.4f)" % (lay[0], lay[1], st, step_base))
+        if st < step_base * MARGIN:
+            layout, step_base = lay, st
+    eng.set_layout(*layout)
     _, step_plain = measure(eng, x, s, y)
     fuse = 0
     eng.set_fusion(True)
@@ -161,6 +173,10 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
                                                     "" if "xy_fused" in times_f else " (no fused kernel)"))
     eng.close()
     fields = ["%d %d %d %d %d" % (prec, fmt, nx, ny, nz), "fuse=%d" % fuse]
+    if layout[0]:
+        fields.append("pad=1")
+    if not layout[1]:
+        fields.append("flat=0")
     if ex:
         fields.append("e_x=%d" % ex)
     if ey:
@@ -192,7 +208,7 @@ def main():
     lines = ["# GB300 tuning cache written by tune.py: prec format nx ny nz key=value ...",
              "# keys: fuse, e_x/e_y/e_z (points per thread of the axis plans), lines per CTA per pass,",
              "# pipe_<pass> (tile buffers of the pipelined kernel), cl_<pass> / cls_<pass> (cluster",
-             "# launch: CTAs a cluster / start barrier)"]
+             "# launch: CTAs a cluster / start barrier), pad / flat (row layout)"]
     for shp in shapes:
         print("shape", shp, flush=True)
         line, ms = tune_shape(*shp)
