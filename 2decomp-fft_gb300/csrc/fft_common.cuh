@@ -28,16 +28,22 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
 }
 // a * (-i)
 template <typename C> __device__ __forceinline__ C cmul_mi(C a) { return cmk<C>(a.y, -a.x); }
+// FP32: one packed two-lane add (FADD2) per complex add or subtract, rounded
+// exactly as the two scalar adds.  A swapped or negated pair (a * -i) as an
+// operand would cost register moves, so the butterflies below write
+// t +/- (-i) d component-wise.
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 
 // ---------------------------------------------------------------------------
 // Forward butterflies (sign -1), natural order in and out.
 // ---------------------------------------------------------------------------
 template <typename C> __device__ __forceinline__ void dft4v(C& a0, C& a1, C& a2, C& a3) {
-  C t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = cmul_mi(csub(a1, a3));
+  C t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), d = csub(a1, a3);
   a0 = cadd(t0, t2);
   a2 = csub(t0, t2);
-  a1 = cadd(t1, t3);
-  a3 = csub(t1, t3);
+  a1 = cmk<C>(t1.x + d.y, t1.y - d.x);  // t1 + (-i) d
+  a3 = cmk<C>(t1.x - d.y, t1.y + d.x);  // t1 - (-i) d
 }
 
 template <typename C> __device__ __forceinline__ void dft2p(C* v) {
@@ -122,8 +128,8 @@ template <typename C> __device__ __forceinline__ void dft8p(C* v) {
   v[4] = csub(e0, o0);
   v[1] = cadd(e1, o1);
   v[5] = csub(e1, o1);
-  v[2] = cadd(e2, o2);
-  v[6] = csub(e2, o2);
+  v[2] = cmk<C>(e2.x + o2.x, e2.y + o2.y);  // o2 = -i v[5]: component-wise
+  v[6] = cmk<C>(e2.x - o2.x, e2.y - o2.y);
   v[3] = cadd(e3, o3);
   v[7] = csub(e3, o3);
 }
@@ -178,7 +184,12 @@ template <typename C> __device__ __forceinline__ void dft32p(C* v) {
     C w;
     if (k <= 8) w = cmk<C>(c[k], -c[8 - k]);
     else w = cmk<C>(-c[16 - k], -c[k - 8]);
-    C t = (k == 0) ? o[k] : (k == 8 ? cmul_mi(o[k]) : cmul(o[k], w));
+    if (k == 8) {  // t = -i o
+      v[k] = cmk<C>(e[k].x + o[k].y, e[k].y - o[k].x);
+      v[k + 16] = cmk<C>(e[k].x - o[k].y, e[k].y + o[k].x);
+      continue;
+    }
+    C t = (k == 0) ? o[k] : cmul(o[k], w);
     v[k] = cadd(e[k], t);
     v[k + 16] = csub(e[k], t);
   }
