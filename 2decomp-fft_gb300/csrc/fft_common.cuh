@@ -458,6 +458,10 @@ struct LineCtx {
     const int a = CONTIG ? line * N + n : n * L + line;
     return a + (a >> 4);
   }
+  // Slot of point n + 16 c is sidx(n) + c * sstep16() (n >= 0): 16 c points
+  // span 16 c entries (contiguous) or 16 c L (strided), plus one pad slot per
+  // 16 entries.
+  __device__ __forceinline__ int sstep16() const { return CONTIG ? 17 : 17 * L; }
   // slot of point n of any line of the tile (same layout as sidx)
   __device__ __forceinline__ int sidx_at(int line_, int n) const {
     const int a = CONTIG ? line_ * N + n : n * L + line_;

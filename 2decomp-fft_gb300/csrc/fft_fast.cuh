@@ -92,6 +92,13 @@ __device__ __forceinline__ void run_plan(const Ctx& c, C* Sm, C (&v)[P::E]) {
       for (int m = 0; m < MB; ++m)
 #pragma unroll
         for (int r = 0; r < R; ++r) v[m * R + r] = c.gload(t + m * TPL + r * NB);
+    } else if constexpr (TPL % 16 == 0 && NB % 16 == 0) {
+      // every point is t + 16 c: one slot computation, then constant steps
+      const int s0 = c.sidx(t), st = c.sstep16();
+#pragma unroll
+      for (int m = 0; m < MB; ++m)
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[m * R + r] = Sm[s0 + ((m * TPL + r * NB) / 16) * st];
     } else {
 #pragma unroll
       for (int m = 0; m < MB; ++m)
@@ -130,10 +137,22 @@ __device__ __forceinline__ void run_plan(const Ctx& c, C* Sm, C (&v)[P::E]) {
         const int b = t + m * TPL;
         const int k = b % NS;
         const int base = (b - k) * R + k;
+        if constexpr (LAST && KIND == K_R2C) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          if constexpr (LAST && KIND == K_R2C) c.put_r2c(Sm, base + r * NS, v[m * R + r]);
-          else Sm[c.sidx(base + r * NS)] = v[m * R + r];
+          for (int r = 0; r < R; ++r) c.put_r2c(Sm, base + r * NS, v[m * R + r]);
+        } else if constexpr (NS % 16 == 0) {
+          // points base + 16 (r NS / 16)
+          const int s0 = c.sidx(base), st = c.sstep16();
+#pragma unroll
+          for (int r = 0; r < R; ++r) Sm[s0 + r * (NS / 16) * st] = v[m * R + r];
+        } else if constexpr (NS == 1 && R % 16 == 0 && Ctx::contiguous) {
+          // base = b R is a multiple of 16, and so is the line's first entry
+          const int s0 = c.sidx(base);
+#pragma unroll
+          for (int r = 0; r < R; ++r) Sm[s0 + r + (r >> 4)] = v[m * R + r];
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; ++r) Sm[c.sidx(base + r * NS)] = v[m * R + r];
         }
       }
       // the r2c split after the last stage reads other lines' points
