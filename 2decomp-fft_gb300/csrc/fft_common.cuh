@@ -622,6 +622,25 @@ struct LineCtx {
       if (has1) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
     }
   }
+  // The same with the line length NN and its TPL threads known at compile
+  // time: every iteration unrolled.
+  template <int NN, int TPL>
+  __device__ __forceinline__ void store_r2c_pairs_ct(const C* S) const {
+    if (!valid) return;
+    const Pair* P = reinterpret_cast<const Pair*>(S);
+    C* d = reinterpret_cast<C*>(dst);
+    const T h = T(0.5);
+    constexpr int J = (NN / 2 + TPL) / TPL;
+#pragma unroll
+    for (int i = 0; i < J; ++i) {
+      const int k = t + i * TPL;
+      if (2 * k > NN) break;
+      const Pair p = P[sstage(k)];
+      const C zk = p.a, zm = p.b;
+      d[db0 + k * dsn] = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
+      if (has1) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
+    }
+  }
 
   // r2c output: separate the two half spectra held in shared memory,
   // X1 = (Z_k + conj Z_{n-k}) / 2, X2 = (Z_k - conj Z_{n-k}) / (2i).

@@ -196,9 +196,15 @@ __global__ void __launch_bounds__(fast_max_threads(E, sizeof(T)), 1)
   if (a.csync) cooperative_groups::this_cluster().sync();
   LineCtx<T, KIND, CONTIG> c;
   c.init(a);
+  // the block is (TPL, L) or (L, TPL): the compiler may fold the per-point
+  // conditions of the c2r gather and the r2c split that depend on t.
+  // Measured per kernel: faster on contiguous lines and strided 1024-point
+  // lines, slower on strided 512-point lines (128 registers instead of 112,
+  // z pass 0.76 -> 0.86 ms on 1024 x 1024 x 512) and 256-point ones.
+  if constexpr (CONTIG || N == 1024) __builtin_assume(c.t >= 0 && c.t < N / E);
   Cx<T> v[E];
   run_stages<N, E, 0>(c, Sm, v);
-  if constexpr (KIND == K_R2C) c.store_r2c_pairs(Sm);
+  if constexpr (KIND == K_R2C) c.template store_r2c_pairs_ct<N, N / E>(Sm);
 }
 
 template <typename T, int KIND, bool CONTIG, int N, int E>
