@@ -379,8 +379,11 @@ __device__ __forceinline__ void dftg(C* v) {
 // Per-thread view of one line: shared-memory slots and global addressing.
 // ---------------------------------------------------------------------------
 // CG: read sources through L2 only (ld.global.cg), for data other CTAs of
-// the same kernel wrote moments earlier.
-template <typename T, int KIND, bool CONTIG, bool CG = false>
+// the same kernel wrote moments earlier.  PRED: loads of padding lines are
+// predicated off (and read as zero); without it a padding line loads the
+// line it is clamped to (see init_at) and only its stores are skipped --
+// which of the two is faster depends on the kernel, as measured.
+template <typename T, int KIND, bool CONTIG, bool CG = false, bool PRED = true>
 struct LineCtx {
   using C = Cx<T>;
   using real_t = T;
@@ -419,6 +422,17 @@ struct LineCtx {
     t = t_;
     line = line_;
     valid = cl < limit;
+    // a padding line is clamped to the last line before `limit` (line 0 of
+    // the first plane when there is none): its addresses stay in bounds, so
+    // that without PRED its loads need no predicate
+    if (!valid) {
+      if (limit > 0) {
+        cl = limit - 1;
+      } else {
+        cl = 0;
+        v = 0;
+      }
+    }
     if (KIND == K_C2C) {
       has1 = false;
       sb0 = CONTIG ? cl * a.s_src_l : cl + v * a.s_src_l;
@@ -492,7 +506,7 @@ struct LineCtx {
   }
 
   __device__ __forceinline__ C gload(int n) const {
-    if (!valid) return cmk<C>(T(0), T(0));
+    if (PRED && !valid) return cmk<C>(T(0), T(0));
     if (KIND == K_C2C) {
       C x = ld(reinterpret_cast<const C*>(src) + sb0 + n * ssn);
       if (inverse) x.y = -x.y;
@@ -568,7 +582,7 @@ struct LineCtx {
 #pragma unroll
     for (int i = 0; i < J; ++i) {
       const int j = t + i * TPL;
-      const bool in = valid && j < h;
+      const bool in = (!PRED || valid) && j < h;
       a[i] = in ? ld(s + sb0 + j * ssn) : cmk<C>(T(0), T(0));
       b[i] = (in && has1) ? ld(s + sb1 + j * ssn) : cmk<C>(T(0), T(0));
     }
