@@ -662,6 +662,11 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst, lo
   // even (every line then starts at an even real index)
   const void* real_ptr = kind == K_R2C ? src : dst;
   a.pair_vec = (!P.contiguous && nx % 2 == 0 && ((uintptr_t)real_ptr % (2 * (size_t)e->prec)) == 0) ? 1 : 0;
+  // FP32 complex pairs: both complex lines of a pair side by side, 16-byte
+  // aligned (every pair starts at an even complex index of an even pitch)
+  const void* cplx_ptr = kind == K_R2C ? dst : src;
+  if (a.pair_vec && e->prec == GBFFT_PREC_SINGLE && cp % 2 == 0 && ((uintptr_t)cplx_ptr % 16) == 0)
+    a.pair_vec |= 2;
   const int axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, kind,
             e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R], e->form == GBFFT_FORM_SPLIT,

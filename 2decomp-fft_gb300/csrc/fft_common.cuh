@@ -394,7 +394,7 @@ struct LineCtx {
   void* dst;
   long long sb0, sb1, db0, db1, ssn, dsn;
   int N, L, tpl, t, line;
-  bool valid, has1, inverse, pvec;
+  bool valid, has1, inverse, pvec, cvec;
 
   __device__ __forceinline__ void init(const PassArgs& a) {
     if (CONTIG)
@@ -418,7 +418,8 @@ struct LineCtx {
     inverse = a.inverse != 0;
     ssn = a.s_src_n;
     dsn = a.s_dst_n;
-    pvec = !CONTIG && a.pair_vec;
+    pvec = !CONTIG && (a.pair_vec & 1);
+    cvec = !CONTIG && std::is_same<T, float>::value && (a.pair_vec & 2);
     t = t_;
     line = line_;
     valid = cl < limit;
@@ -505,6 +506,11 @@ struct LineCtx {
     }
   }
 
+  __device__ __forceinline__ static float4 ld4(const float4* p) {
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+  }
+
   __device__ __forceinline__ C gload(int n) const {
     if (PRED && !valid) return cmk<C>(T(0), T(0));
     if (KIND == K_C2C) {
@@ -583,6 +589,14 @@ struct LineCtx {
     for (int i = 0; i < J; ++i) {
       const int j = t + i * TPL;
       const bool in = (!PRED || valid) && j < h;
+      if constexpr (std::is_same<T, float>::value) {
+        if (cvec && has1) {  // the pair's two complex values side by side
+          const float4 q = in ? ld4(reinterpret_cast<const float4*>(s + sb0 + j * ssn)) : make_float4(0.f, 0.f, 0.f, 0.f);
+          a[i] = cmk<C>(q.x, q.y);
+          b[i] = cmk<C>(q.z, q.w);
+          continue;
+        }
+      }
       a[i] = in ? ld(s + sb0 + j * ssn) : cmk<C>(T(0), T(0));
       b[i] = (in && has1) ? ld(s + sb1 + j * ssn) : cmk<C>(T(0), T(0));
     }
@@ -651,8 +665,16 @@ struct LineCtx {
       if (2 * k > NN) break;
       const Pair p = P[sstage(k)];
       const C zk = p.a, zm = p.b;
-      d[db0 + k * dsn] = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
-      if (has1) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
+      const C x1 = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
+      const C x2 = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
+      if constexpr (std::is_same<T, float>::value) {
+        if (cvec && has1) {  // the pair's two complex outputs side by side
+          *reinterpret_cast<float4*>(d + db0 + k * dsn) = make_float4(x1.x, x1.y, x2.x, x2.y);
+          continue;
+        }
+      }
+      d[db0 + k * dsn] = x1;
+      if (has1) d[db1 + k * dsn] = x2;
     }
   }
 

@@ -64,7 +64,7 @@ __device__ __forceinline__ void issue_tile(const PassArgs& a, Cx<T>* S, long lon
     }
   } else if constexpr (KIND == K_R2C) {
     const T* src = reinterpret_cast<const T*>(a.src);
-    const bool pv = !CONTIG && a.pair_vec;
+    const bool pv = !CONTIG && (a.pair_vec & 1);
     for (int e = tid; e < N * L; e += nthreads) {
       const int line = CONTIG ? e / N : (e & (L - 1));
       const int n = CONTIG ? (e & (N - 1)) : (e >> lg);

@@ -59,8 +59,10 @@ struct PassArgs {
   int fast;        // 1: compile-time power-of-two kernel, 2: mixed-radix kernel,
                    // 3: split-precision tensor-core kernel, 4: balanced
                    // non-power-of-two plan
-  int pair_vec;    // r2c/c2r on strided lines: the two real lines of a pair
-                   // are adjacent and 8-byte aligned (read/write as one pair)
+  int pair_vec;    // r2c/c2r on strided lines, bit 0: the two real lines of a
+                   // pair are adjacent and aligned (read/write as one pair);
+                   // bit 1 (FP32): so are their two complex lines, 16-byte
+                   // aligned (one 16-byte access for both)
   int pipe;        // fast == 1: 0 = one-shot kernel, 2 or 3 = pipelined
                    // persistent kernel with that many tile buffers
   int csize;       // fast == 1, one-shot: 0, or launch CTAs in clusters of
