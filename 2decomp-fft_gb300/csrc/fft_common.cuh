@@ -382,7 +382,8 @@ __device__ __forceinline__ void dftg(C* v) {
 // the same kernel wrote moments earlier.  PRED: loads of padding lines are
 // predicated off (and read as zero); without it a padding line loads the
 // line it is clamped to (see init_at) and only its stores are skipped --
-// which of the two is faster depends on the kernel, as measured.
+// faster in the power-of-two kernel, slower in the balanced and
+// mixed-radix ones (measured).
 template <typename T, int KIND, bool CONTIG, bool CG = false, bool PRED = true>
 struct LineCtx {
   using C = Cx<T>;

@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(fast_max_threads(E, sizeof(T)), 1)
   // launched in clusters: start together, so that neighbouring CTAs' loads
   // of the same rows are in the DRAM queues at the same time
   if (a.csync) cooperative_groups::this_cluster().sync();
-  // unpredicated padding-line loads: faster here except on strided c2r tiles
-  LineCtx<T, KIND, CONTIG, false, KIND == K_C2R && !CONTIG> c;
+  // unpredicated padding-line loads
+  LineCtx<T, KIND, CONTIG, false, false> c;
   c.init(a);
   // the block is (TPL, L) or (L, TPL): the compiler may fold the per-point
   // conditions of the c2r gather and the r2c split that depend on t.
