@@ -256,6 +256,105 @@ __global__ void __launch_bounds__(fast_max_threads(16, sizeof(T)), 1)
   }
 }
 
+// Extension length M = R0 * R1 (dtt_mixed_length): the two-stage plan of the
+// mixed-radix passes (fft_mixed.cuh) on the extension in one padded shared
+// buffer.  R1 threads a line: stage 0 radix R0 (butterfly t, points t + r R1),
+// stage 1 radix R1 (threads t < R0, points t + r R0, twiddles from the
+// stage-major table a.twf), in place.
+template <typename T, bool CONTIG, int M>
+__global__ void __launch_bounds__(256) dtt_mixed_kernel(const __grid_constant__ DttArgs a) {
+  using C = Cx<T>;
+  constexpr int R0 = mixed_r0(M), R1 = M / R0;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* Sm = reinterpret_cast<C*>(smem_raw);
+  int t, line;
+  long long u, v;
+  if (CONTIG) {
+    t = threadIdx.x;
+    line = threadIdx.y;
+    u = (long long)blockIdx.x * a.L + line;
+    v = 0;
+  } else {
+    line = threadIdx.x;
+    t = threadIdx.y;
+    u = (long long)blockIdx.x * a.L + line;
+    v = blockIdx.y;
+  }
+  const bool valid = u < a.nlines;
+  const long long base = CONTIG ? u * a.sl : u + v * a.sl;
+  const T* src = reinterpret_cast<const T*>(a.src);
+  T* dst = reinterpret_cast<T*>(a.dst);
+  const int n = a.n, kind = a.kind;
+  const C* w4 = reinterpret_cast<const C*>(a.w4);
+  const C* tw = reinterpret_cast<const C*>(a.twf);
+  LineCtx<T, K_C2C, CONTIG> c;
+  c.N = M;
+  c.L = a.L;
+  c.t = t;
+  c.tpl = R1;
+  c.line = line;
+  auto X = [&](int j) -> T { return valid ? src[base + (long long)(a.off + j) * a.sn] : T(0); };
+#pragma unroll 1
+  for (int m = t; m < M; m += R1) Sm[c.sidx(m)] = extension<C>(kind, m, n, M, X, w4);
+  __syncthreads();
+  C x[R1];
+  // stage 0: radix R0, butterfly t, points t + r R1
+#pragma unroll
+  for (int r = 0; r < R0; ++r) x[r] = Sm[c.sidx(t + r * R1)];
+  dftg<R0>(x);
+  __syncthreads();  // every point read before the stage's outputs overwrite them
+#pragma unroll
+  for (int r = 0; r < R0; ++r) Sm[c.sidx(t * R0 + r)] = x[r];
+  __syncthreads();
+  // stage 1: radix R1 after R0 points, butterflies t < R0, in place
+  if (t < R0) {
+#pragma unroll
+    for (int r = 0; r < R1; ++r) x[r] = Sm[c.sidx(t + r * R0)];
+#pragma unroll
+    for (int r = 1; r < R1; ++r) x[r] = cmul(x[r], tw[(R0 - 1) + (r - 1) * R0 + t]);
+    dftg<R1>(x);
+#pragma unroll
+    for (int r = 0; r < R1; ++r) Sm[c.sidx(t + r * R0)] = x[r];
+  }
+  __syncthreads();
+  if (!valid) return;
+  const C c0 = cmk<C>(T(a.c0x), T(a.c0y));
+#pragma unroll 1
+  for (int k = t; k < n; k += R1)
+    dst[base + (long long)(a.off + k) * a.sn] = output<C>(kind, k, n, [&](int i) { return Sm[c.sidx(i)]; }, w4, c0);
+  if (a.src != a.dst) {
+#pragma unroll 1
+    for (int j = t; j < a.naxis; j += R1)
+      if (j < a.off || j >= a.off + n) dst[base + (long long)j * a.sn] = src[base + (long long)j * a.sn];
+  }
+}
+
+template <typename T, bool CONTIG, int M>
+cudaError_t launch_mixed_m(const DttArgs& a, cudaStream_t stream) {
+  constexpr int TPL = M / mixed_r0(M);
+  if (a.tpl != TPL || a.L * TPL > 256) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)fast_smem_entries(M, a.L) * sizeof(Cx<T>);
+  auto kern = dtt_mixed_kernel<T, CONTIG, M>;
+  if (smem > 48 * 1024) {
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+  }
+  const dim3 block = CONTIG ? dim3(TPL, a.L) : dim3(a.L, TPL);
+  const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
+  kern<<<grid, block, smem, stream>>>(a);
+  add_launches(1);
+  return cudaGetLastError();
+}
+
+template <typename T, bool CONTIG>
+cudaError_t launch_mixed(const DttArgs& a, cudaStream_t s) {
+  switch (a.M) {
+    case 126: return launch_mixed_m<T, CONTIG, 126>(a, s);
+    case 510: return launch_mixed_m<T, CONTIG, 510>(a, s);
+    default: return cudaErrorNotSupported;
+  }
+}
+
 template <typename T, bool CONTIG, int M>
 cudaError_t launch_fast_m(const DttArgs& a, cudaStream_t stream) {
   constexpr int TPL = M / 16;
@@ -311,6 +410,10 @@ size_t dtt_smem_bytes(int prec_bytes, int M, int L) {
 
 cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream) {
   if (a.n < 1 || a.M < 2 || a.L < 1 || a.tpl < 1) return cudaErrorInvalidValue;
+  if (a.twf && dtt_mixed_length(a.M)) {
+    if (prec_bytes == 4) return contiguous ? launch_mixed<float, true>(a, stream) : launch_mixed<float, false>(a, stream);
+    return contiguous ? launch_mixed<double, true>(a, stream) : launch_mixed<double, false>(a, stream);
+  }
   if (a.twf) {
     if (!dtt_fast_length(a.M)) return cudaErrorInvalidValue;
     if (prec_bytes == 4) return contiguous ? launch_fast<float, true>(a, stream) : launch_fast<float, false>(a, stream);

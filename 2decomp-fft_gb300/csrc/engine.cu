@@ -1411,9 +1411,17 @@ int setup_dtt_axis(DttAxis& a, int kind, int first, int ndismiss, int naxis, int
     return fail(GBFFT_ERR_UNSUPPORTED, "r2r extension does not fit one shared-memory tile");
   int rc = upload_table(&a.tw, twiddles(a.M), prec);
   if (rc != GBFFT_OK) return rc;
-  if (dtt_fast_length(a.M)) {
+  // the two-stage plan in FP32 only: in FP64 its 30-point butterflies take
+  // 210 registers a thread and the 510-point pass ran slower than the
+  // runtime-planned one
+  const bool mixed = dtt_mixed_length(a.M) && prec == GBFFT_PREC_SINGLE;
+  if (dtt_fast_length(a.M) || mixed) {
     std::vector<int> radices;
-    for (int s = 0; s < fast_nst(a.M, 16); ++s) radices.push_back(fast_radix(a.M, 16, s));
+    if (mixed) {
+      radices = {mixed_r0(a.M), a.M / mixed_r0(a.M)};
+    } else {
+      for (int s = 0; s < fast_nst(a.M, 16); ++s) radices.push_back(fast_radix(a.M, 16, s));
+    }
     rc = upload_table(&a.twf, stage_twiddles(radices), prec);
     if (rc != GBFFT_OK) return rc;
   }
@@ -1549,6 +1557,20 @@ int gbfft_exec_r2r(gbfft_dtt_t d, void* d_in, void* d_out, int isign, void* stre
       a.naxis = (int)nz;
     }
     if (!contiguous && a.nv > 65535) return fail(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
+    if (ax.twf && dtt_mixed_length(ax.M)) {
+      // compile-time two-stage plan: R1 threads a line, at most 256 a CTA;
+      // contiguous about 128, strided up to 16 neighbouring lines
+      const int tplm = ax.M / mixed_r0(ax.M);
+      int Lm = contiguous ? (tplm >= 128 ? 1 : 128 / tplm) : 16;
+      while (Lm > 1 && Lm * tplm > 256) --Lm;
+      while (Lm > 1 && (size_t)fast_smem_entries(ax.M, Lm) * 2 * d->prec > 100 * 1024) --Lm;
+      if (a.nlines < Lm) Lm = (int)a.nlines;
+      a.L = Lm;
+      a.tpl = tplm;
+      cudaError_t err = launch_dtt_pass(d->prec, contiguous, a, st);
+      if (err != cudaSuccess) return cuda_fail(err, "r2r pass launch");
+      continue;
+    }
     if (ax.twf) {
       // compile-time 16-point plan: M / 16 threads a line; contiguous
       // 128-thread CTAs, strided up to 16 neighbouring lines

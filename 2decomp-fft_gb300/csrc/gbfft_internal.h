@@ -256,6 +256,11 @@ struct DttArgs {
 size_t dtt_smem_bytes(int prec_bytes, int M, int L);
 // power-of-two extension lengths with a compile-time plan for the r2r pass
 __host__ __device__ constexpr bool dtt_fast_length(int M) { return M >= 32 && M <= 2048 && (M & (M - 1)) == 0; }
+// Extension lengths with the compile-time two-stage plan M = R0 * R1
+// (mixed_r0): 126 = 9 * 14 and 510 = 17 * 30, the default windows of every
+// kind on axes of 64 and 256 points (FP32; the engine keeps FP64 on the
+// runtime plan).
+__host__ __device__ constexpr bool dtt_mixed_length(int M) { return M == 126 || M == 510; }
 cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream);
 
 // Enqueue one axis pass.  prec_bytes = 4 (float) or 8 (double).

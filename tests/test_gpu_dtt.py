@@ -191,3 +191,27 @@ def test_round_trip_all_512_combinations_power_of_two_extensions(fmt):
             sl.append(slice(cfg[3 + d] - 1, n - cfg[6 + d] + cfg[3 + d] - 1))
         assert np.abs(back - a0)[tuple(sl)].max() <= 100 * eps, kinds
         e.close()
+
+
+# Axes of 64 and 256 points: every kind's default window has an extension
+# of 126 = 9 * 14 or 510 = 17 * 30 points, which runs the compile-time
+# two-stage plan in FP32 (and the runtime plan in FP64).
+@pytest.mark.parametrize("prec", [8, 4])
+@pytest.mark.parametrize("fmt", [1, 3])
+@pytest.mark.parametrize("shape", [(256, 12, 10), (10, 256, 6), (6, 10, 256), (64, 64, 9)])
+def test_r2r_two_stage_extensions_against_oracle(prec, fmt, shape):
+    import gbfft
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx + 2 * ny + 3 * nz + fmt)
+    for k in range(1, 9):
+        kinds = [k, k, k]
+        a = rng.standard_normal((nz, ny, nx))
+        cfg = D.config(kinds)
+        e = gbfft.Dtt(fmt, nx, ny, nz, kinds, prec=prec)
+        for isign in (-1, 1):
+            x = torch.from_numpy(a).to(dtype(prec)).cuda()
+            out = torch.empty_like(x)
+            e.r2r(x, out, isign)
+            _, ref = D.dtt_3d_r2r(a, fmt, cfg, isign)
+            assert rel(out.cpu().numpy(), ref) <= TOL[prec], (k, isign)
+        e.close()
