@@ -777,8 +777,9 @@ namespace {
 
 // The passes of a 3D r2c (src/fft_common_3d.f90:121-189): the r2c pass
 // along the real axis into `out`, then the c2c passes on `out`.
-// With a work area, every pass but the last writes it (rows padded to
-// aligned starts) and the last one writes `out`.
+// With the padded layout every pass but the last writes the work area (rows
+// padded to aligned starts) and the last one writes `out`; otherwise all
+// passes work in `out`, which needs no work area.
 std::vector<Pass> r2c_passes(gbfft_engine_s* e, const void* d_in, void* d_out) {
   std::vector<Pass> ps;
   const int s1 = e->sp[0], s2 = e->sp[1], s3 = e->sp[2];
@@ -787,7 +788,7 @@ std::vector<Pass> r2c_passes(gbfft_engine_s* e, const void* d_in, void* d_out) {
   int axes[2], na = 0;
   for (int i = 0; i < 2; ++i)
     if (!e->skip[order[i]]) axes[na++] = order[i];
-  void* W = e->inplace ? nullptr : e->work;
+  void* W = (!e->inplace && e->pad) ? e->work : nullptr;
   const long long wp = W ? work_pitch(e) : s1;
   void* mid = W ? W : d_out;
   ps.push_back(real_pass(e, K_R2C, d_in, na ? mid : d_out, na ? wp : s1));

@@ -140,7 +140,7 @@ def test_tile_shapes_give_the_same_transform():
 def test_cache_line_is_applied(tmp_path):
     import gbfft
     path = tmp_path / "cache.txt"
-    path.write_text("# test\n4 1 64 1024 512 fuse=0 e_y=16 e_z=32 c2c_y=4 r2c=2\n")
+    path.write_text("# test\n4 1 64 1024 512 fuse=0 e_y=16 e_z=32 c2c_y=4 r2c=2 pad=1 flat=0\n")
     gbfft.set_tune_cache(str(path))
     try:
         e = gbfft.Engine(1, 64, 1024, 512, prec=gbfft.PREC_SINGLE)
@@ -148,9 +148,11 @@ def test_cache_line_is_applied(tmp_path):
         assert t["points"][1:] == (16, 32)
         assert t["tiles"]["c2c_y"] == 4 and t["tiles"]["r2c"] == 2
         assert t["fuse"] is False
+        assert e.layout() == (True, False)
         e.close()
         other = gbfft.Engine(1, 64, 1024, 256, prec=gbfft.PREC_SINGLE)
         assert other.tuning()["tiles"]["c2c_y"] == 0  # no line for this shape
+        assert other.layout() == (False, True)  # the built-in layout
         other.close()
     finally:
         gbfft.set_tune_cache(None)
