@@ -305,13 +305,14 @@ struct gbfft_engine_s {
   long long sync_planes = 0;
   void* work = nullptr;
   size_t work_bytes = 0;
-  // Row layout: `pad` -- the work area's rows of complex values start on
+  // Row layout: `pad` -- 1: the work area's rows of complex values start on
   // kRowAlignBytes boundaries (its row pitch is sp[0] rounded up) and every
   // r2c / c2r pass but the last writes there, so that the strided passes
-  // store whole 32-byte sectors; `flat` -- z passes whose output rows are
+  // store whole 32-byte sectors; 2: the same for c2r only (r2c works in its
+  // output); 0: unpadded.  `flat` -- z passes whose output rows are
   // unpadded and not so aligned take the lines of each (x, y) plane flat
   // (segments aligned as the plane is).
-  bool pad = false;
+  int pad = 0;
   bool flat = true;
 };
 
@@ -349,6 +350,7 @@ long long padded_pitch(const gbfft_engine_s* e) {
   const long long q = (long long)(kRowAlignBytes / cbytes(e));
   return (e->sp[0] + q - 1) / q * q;
 }
+// pitch of the work area's rows for c2r (r2c uses the work area only with pad 1)
 long long work_pitch(const gbfft_engine_s* e) { return e->pad ? padded_pitch(e) : e->sp[0]; }
 // Rows of n elements of `bytes` each whose tiles of 16 lines start on
 // 32-byte sectors and fill each row: taken per row, a z pass over them is
@@ -788,7 +790,7 @@ std::vector<Pass> r2c_passes(gbfft_engine_s* e, const void* d_in, void* d_out) {
   int axes[2], na = 0;
   for (int i = 0; i < 2; ++i)
     if (!e->skip[order[i]]) axes[na++] = order[i];
-  void* W = (!e->inplace && e->pad) ? e->work : nullptr;
+  void* W = (!e->inplace && e->pad == 1) ? e->work : nullptr;
   const long long wp = W ? work_pitch(e) : s1;
   void* mid = W ? W : d_out;
   ps.push_back(real_pass(e, K_R2C, d_in, na ? mid : d_out, na ? wp : s1));
@@ -985,7 +987,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
       e->csync[k] = 0;
     }
   if (tune.fuse >= 0) e->fuse = tune.fuse != 0;
-  if (tune.pad >= 0) e->pad = tune.pad != 0;
+  if (tune.pad >= 0 && tune.pad <= 2) e->pad = tune.pad;
   if (tune.flat >= 0) e->flat = tune.flat != 0;
   g_err.clear();
   *engine = e;
@@ -1283,14 +1285,15 @@ int gbfft_engine_get_tuning(gbfft_engine_t e, int* fuse, int* tiles, int* points
 
 int gbfft_engine_set_layout(gbfft_engine_t e, int pad, int flat) {
   if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
-  e->pad = pad != 0;
+  if (pad < 0 || pad > 2) return fail(GBFFT_ERR_INVALID, "pad must be 0, 1 or 2");
+  e->pad = pad;
   e->flat = flat != 0;
   return GBFFT_OK;
 }
 
 int gbfft_engine_get_layout(gbfft_engine_t e, int* pad, int* flat) {
   if (!valid_engine(e) || !pad || !flat) return fail(GBFFT_ERR_INVALID, "bad argument");
-  *pad = e->pad ? 1 : 0;
+  *pad = e->pad;
   *flat = e->flat ? 1 : 0;
   return GBFFT_OK;
 }

@@ -290,16 +290,17 @@ class Engine:
         d = (ctypes.c_int * len(PASS_NAMES))()
         check(lib().gbfft_engine_get_pipeline(self.h, d))
         return dict(zip(PASS_NAMES, d))
-    def set_layout(self, pad=True, flat=True):
-        """Padded work-area rows (aligned row segments for the strided passes;
-        default off) and flat z passes over unpadded misaligned planes
-        (default on)."""
-        check(lib().gbfft_engine_set_layout(self.h, int(bool(pad)), int(bool(flat))))
+    def set_layout(self, pad=1, flat=True):
+        """Padded work-area rows (aligned row segments for the strided passes):
+        pad 1 (or True) for r2c and c2r, 2 for c2r only, 0 (default) none;
+        flat z passes over unpadded misaligned planes (default on)."""
+        check(lib().gbfft_engine_set_layout(self.h, int(pad), int(bool(flat))))
 
     def layout(self):
+        """(pad, flat): pad 0, 1 or 2, flat a bool."""
         p, f = ctypes.c_int(), ctypes.c_int()
         check(lib().gbfft_engine_get_layout(self.h, ctypes.byref(p), ctypes.byref(f)))
-        return bool(p.value), bool(f.value)
+        return p.value, bool(f.value)
 
     def set_fusion(self, enable):
         """Fuse the x and y passes of each z-plane into one kernel (default on)."""

@@ -154,9 +154,9 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
             eng.set_cluster(kind, *c)
     # row layout, the built-in one (unpadded rows, flat z passes over
     # misaligned planes) unless another wins the step by 1 %
-    layout = (False, True)
+    layout = (0, True)
     _, step_base = measure(eng, x, s, y)
-    for lay in ((True, True), (False, False), (True, False)):
+    for lay in ((1, True), (2, True), (0, False), (1, False)):
         eng.set_layout(*lay)
         _, st = measure(eng, x, s, y)
         log("  layout pad=%d flat=%d: %.4f ms (built-in %.4f)" % (lay[0], lay[1], st, step_base))
@@ -174,7 +174,7 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     eng.close()
     fields = ["%d %d %d %d %d" % (prec, fmt, nx, ny, nz), "fuse=%d" % fuse]
     if layout[0]:
-        fields.append("pad=1")
+        fields.append("pad=%d" % layout[0])
     if not layout[1]:
         fields.append("flat=0")
     if ex:

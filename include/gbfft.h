@@ -196,17 +196,18 @@ int gbfft_engine_get_pipeline(gbfft_engine_t engine, int* depth);
 int gbfft_engine_set_cluster(gbfft_engine_t engine, int kind, int ctas, int sync);
 int gbfft_engine_get_cluster(gbfft_engine_t engine, int* ctas, int* sync);
 
-/* Row layout of the passes.  pad = 1: the work area's rows of
- * complex values (sp[0] of them) start on 64-byte boundaries, and every
- * pass of an r2c or c2r but the last writes there, so that the strided
- * passes store whole 32-byte sectors (rows of nx/2+1 values are mostly
- * misaligned otherwise); engines created with inplace have no work area and
- * ignore it; 0 (default) keeps the arrays' own rows.  flat = 1 (default): a
- * z pass whose output rows are unpadded and do not start on 32-byte sectors
- * (or hold a number of values that is not a multiple of 16) takes the lines
- * of each (x, y) plane flat, so that its row segments are as aligned as the
- * plane.  Both are tuning choices (keys pad= and flat= of the tuning
- * cache); the work area is sized for padded rows whatever the setting. */
+/* Row layout of the passes.  pad = 1: the work area's rows of complex values
+ * (sp[0] of them) start on 64-byte boundaries, and every pass of an r2c or
+ * c2r but the last writes there, so that the strided passes store whole
+ * 32-byte sectors (rows of nx/2+1 values are mostly misaligned otherwise);
+ * pad = 2: the same for c2r only, r2c working in its output; pad = 0
+ * (default): the arrays' own rows.  Engines created with inplace have no
+ * work area and ignore it.  flat = 1 (default): a z pass whose output rows
+ * are unpadded and do not start on 32-byte sectors (or hold a number of
+ * values that is not a multiple of 16) takes the lines of each (x, y) plane
+ * flat, so that its row segments are as aligned as the plane.  Both are
+ * tuning choices (keys pad= and flat= of the tuning cache); the work area
+ * is sized for padded rows whatever the setting. */
 int gbfft_engine_set_layout(gbfft_engine_t engine, int pad, int flat);
 int gbfft_engine_get_layout(gbfft_engine_t engine, int* pad, int* flat);
 

@@ -15,7 +15,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 TOL = {"s": 2e-6, "d": 1e-12}
-LAYOUTS = [(True, True), (False, True), (True, False), (False, False)]
+LAYOUTS = [(True, True), (False, True), (True, False), (False, False), (2, True), (2, False)]
 
 
 def rel(a, b):
@@ -94,6 +94,17 @@ def test_layout_overwrite_engine(fmt, prec):
         y = e.empty_physical()
         e.c2r(s, y)
         assert rel(y.cpu().numpy() / (nx * ny * nz), x) <= TOL[prec]
+    e.close()
+
+
+def test_layout_values_are_validated():
+    import gbfft
+    e = gbfft.Engine(1, 32, 16, 8, prec=gbfft.PREC_SINGLE)
+    for bad in (-1, 3):
+        with pytest.raises(gbfft.GbfftError, match="pad"):
+            e.set_layout(bad, True)
+    e.set_layout(2, False)
+    assert e.layout() == (2, False)
     e.close()
 
 
