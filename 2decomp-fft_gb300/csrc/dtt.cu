@@ -411,8 +411,9 @@ size_t dtt_smem_bytes(int prec_bytes, int M, int L) {
 cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream) {
   if (a.n < 1 || a.M < 2 || a.L < 1 || a.tpl < 1) return cudaErrorInvalidValue;
   if (a.twf && dtt_mixed_length(a.M)) {
-    if (prec_bytes == 4) return contiguous ? launch_mixed<float, true>(a, stream) : launch_mixed<float, false>(a, stream);
-    return contiguous ? launch_mixed<double, true>(a, stream) : launch_mixed<double, false>(a, stream);
+    // FP32 only: the engine keeps FP64 on the runtime plan
+    if (prec_bytes != 4) return cudaErrorInvalidValue;
+    return contiguous ? launch_mixed<float, true>(a, stream) : launch_mixed<float, false>(a, stream);
   }
   if (a.twf) {
     if (!dtt_fast_length(a.M)) return cudaErrorInvalidValue;
