@@ -779,6 +779,104 @@ namespace {
 
 // The passes of a 3D r2c (src/fft_common_3d.f90:121-189): the r2c pass
 // along the real axis into `out`, then the c2c passes on `out`.
+// Arguments of an engine: the same checks and order as
+// src/fft_common.f90:157-166, :210-216, and the backend's own limits.
+int check_engine_args(int format, int nx, int ny, int nz, int prec, int form) {
+  if (nx <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for nx");
+  if (ny <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for ny");
+  if (nz <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for nz");
+  if (format != GBFFT_PHYSICAL_IN_X && format != GBFFT_PHYSICAL_IN_Z)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for pencil");
+  if (prec != GBFFT_PREC_SINGLE && prec != GBFFT_PREC_DOUBLE)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for precision (4 or 8)");
+  if (form != GBFFT_FORM_PLAIN && form != GBFFT_FORM_SPLIT)
+    return fail(GBFFT_ERR_INVALID, "Invalid value for form");
+  if (form == GBFFT_FORM_SPLIT && prec != GBFFT_PREC_SINGLE)
+    return fail(GBFFT_ERR_UNSUPPORTED, "the split tensor-core form works on single-precision data");
+  const long long cells = (long long)nx * ny * nz;
+  if (cells > (1LL << 40)) return fail(GBFFT_ERR_UNSUPPORTED, "grid too large");
+  if ((long long)ny * nz > 0x7fffffffLL || (long long)nx * ny > 0x7fffffffLL)
+    return fail(GBFFT_ERR_UNSUPPORTED, "line count exceeds 2^31");
+  return GBFFT_OK;
+}
+
+// The host half of gbfft_engine_create: fields, the axis plans and the
+// tuning-cache line, no device memory (the caller uploads the twiddle tables
+// and allocates the work area).  Arguments are already validated.
+int engine_init_host(gbfft_engine_s* e, int format, int nx, int ny, int nz, int inplace, const int* skip, int prec,
+                     int form, TuneEntry* tune_out) {
+  e->format = format;
+  e->nx = nx;
+  e->ny = ny;
+  e->nz = nz;
+  e->inplace = inplace ? 1 : 0;
+  for (int i = 0; i < 3; ++i) e->skip[i] = skip ? (skip[i] ? 1 : 0) : 0;
+  e->prec = prec;
+  e->form = form;
+  e->ph[0] = nx;
+  e->ph[1] = ny;
+  e->ph[2] = nz;
+  e->sp[0] = format == GBFFT_PHYSICAL_IN_X ? nx / 2 + 1 : nx;
+  e->sp[1] = ny;
+  e->sp[2] = format == GBFFT_PHYSICAL_IN_Z ? nz / 2 + 1 : nz;
+  const TuneEntry tune = lookup_tune(prec, format, nx, ny, nz);
+  const int lens[3] = {nx, ny, nz};
+  for (int d = 0; d < 3; ++d) {
+    std::string why;
+    if (!factorize(lens[d], e->ax[d], why)) return fail(GBFFT_ERR_UNSUPPORTED, why);
+    if (pass_smem_bytes(prec, lens[d], 1) > 200 * 1024)
+      return fail(GBFFT_ERR_UNSUPPORTED, "axis length " + std::to_string(lens[d]) +
+                                             " does not fit one shared-memory tile at this precision");
+    e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
+    if (gen_length(lens[d])) e->ax[d].fast_e = gen_points(lens[d]);
+    if (fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
+    if (gen_length(lens[d]) && (tune.e[d] == gen_points(lens[d]) || tune.e[d] == 2))
+      e->ax[d].fast_e = tune.e[d];
+    if (form == GBFFT_FORM_SPLIT && split_length(lens[d])) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
+  }
+  *tune_out = tune;
+  return GBFFT_OK;
+}
+
+// Tuned tile shapes, launch forms, fusion and row layout for this shape,
+// when the cache has them (host settings only).
+void apply_tune(gbfft_engine_s* e, const TuneEntry& tune) {
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
+    if (tune.L[k] > 0 && gbfft_engine_set_tile(e, k, tune.L[k]) != GBFFT_OK) e->tile_L[k] = 0;
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
+    if (tune.pipe[k] > 0 && gbfft_engine_set_pipeline(e, k, tune.pipe[k]) != GBFFT_OK) e->pipe[k] = 0;
+  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
+    if (tune.csize[k] > 0 && gbfft_engine_set_cluster(e, k, tune.csize[k], tune.csync[k]) != GBFFT_OK) {
+      e->csize[k] = 0;
+      e->csync[k] = 0;
+    }
+  if (tune.fuse >= 0) e->fuse = tune.fuse != 0;
+  if (tune.pad >= 0 && tune.pad <= 2) e->pad = tune.pad;
+  if (tune.flat >= 0) e->flat = tune.flat != 0;
+}
+
+// The passes of a 3D c2c (src/fft_common_3d.f90:9-116): x, y, z (forward
+// in PHYSICAL_IN_X, backward in PHYSICAL_IN_Z) or z, y, x, the first from
+// `in` to `out`, the others in place in `out`; none when every axis is
+// skipped (the call is then a copy).
+std::vector<Pass> c2c_passes(gbfft_engine_s* e, const void* d_in, void* d_out, int isign) {
+  const int n1 = e->nx, n2 = e->ny, n3 = e->nz;
+  const bool x_first = (e->format == GBFFT_PHYSICAL_IN_X && isign == GBFFT_FORWARD) ||
+                       (e->format == GBFFT_PHYSICAL_IN_Z && isign == GBFFT_BACKWARD);
+  const int order_f[3] = {0, 1, 2}, order_b[3] = {2, 1, 0};
+  const int* order = x_first ? order_f : order_b;
+  const int inv = isign == GBFFT_BACKWARD ? 1 : 0;
+  std::vector<Pass> ps;
+  const void* cur = d_in;
+  for (int i = 0; i < 3; ++i) {
+    const int ax = order[i];
+    if (e->skip[ax]) continue;
+    ps.push_back(c2c_pass(e, ax, n1, n2, n3, cur, d_out, inv, n1, n1));
+    cur = d_out;
+  }
+  return ps;
+}
+
 // With the padded layout every pass but the last writes the work area (rows
 // padded to aligned starts) and the last one writes `out`; otherwise all
 // passes work in `out`, which needs no work area.
@@ -890,60 +988,18 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
                         int form, gbfft_engine_t* engine) {
   if (!engine) return fail(GBFFT_ERR_INVALID, "engine output pointer is null");
   *engine = nullptr;
-  // same checks and order as src/fft_common.f90:157-166, :210-216
-  if (nx <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for nx");
-  if (ny <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for ny");
-  if (nz <= 0) return fail(GBFFT_ERR_INVALID, "Invalid value for nz");
-  if (format != GBFFT_PHYSICAL_IN_X && format != GBFFT_PHYSICAL_IN_Z)
-    return fail(GBFFT_ERR_INVALID, "Invalid value for pencil");
-  if (prec != GBFFT_PREC_SINGLE && prec != GBFFT_PREC_DOUBLE)
-    return fail(GBFFT_ERR_INVALID, "Invalid value for precision (4 or 8)");
-  if (form != GBFFT_FORM_PLAIN && form != GBFFT_FORM_SPLIT)
-    return fail(GBFFT_ERR_INVALID, "Invalid value for form");
-  if (form == GBFFT_FORM_SPLIT && prec != GBFFT_PREC_SINGLE)
-    return fail(GBFFT_ERR_UNSUPPORTED, "the split tensor-core form works on single-precision data");
-  const long long cells = (long long)nx * ny * nz;
-  if (cells > (1LL << 40)) return fail(GBFFT_ERR_UNSUPPORTED, "grid too large");
-  if ((long long)ny * nz > 0x7fffffffLL || (long long)nx * ny > 0x7fffffffLL)
-    return fail(GBFFT_ERR_UNSUPPORTED, "line count exceeds 2^31");
-
+  int rc = check_engine_args(format, nx, ny, nz, prec, form);
+  if (rc != GBFFT_OK) return rc;
   gbfft_engine_s* e = new (std::nothrow) gbfft_engine_s();
   if (!e) return fail(GBFFT_ERR_ALLOC, "host allocation failed");
-  e->format = format;
-  e->nx = nx;
-  e->ny = ny;
-  e->nz = nz;
-  e->inplace = inplace ? 1 : 0;
-  for (int i = 0; i < 3; ++i) e->skip[i] = skip ? (skip[i] ? 1 : 0) : 0;
-  e->prec = prec;
-  e->form = form;
-  e->ph[0] = nx;
-  e->ph[1] = ny;
-  e->ph[2] = nz;
-  e->sp[0] = format == GBFFT_PHYSICAL_IN_X ? nx / 2 + 1 : nx;
-  e->sp[1] = ny;
-  e->sp[2] = format == GBFFT_PHYSICAL_IN_Z ? nz / 2 + 1 : nz;
-
-  const TuneEntry tune = lookup_tune(prec, format, nx, ny, nz);
-  const int lens[3] = {nx, ny, nz};
+  TuneEntry tune;
+  rc = engine_init_host(e, format, nx, ny, nz, inplace, skip, prec, form, &tune);
+  if (rc != GBFFT_OK) {
+    delete e;
+    return rc;
+  }
   for (int d = 0; d < 3; ++d) {
-    std::string why;
-    if (!factorize(lens[d], e->ax[d], why)) {
-      delete e;
-      return fail(GBFFT_ERR_UNSUPPORTED, why);
-    }
-    if (pass_smem_bytes(prec, lens[d], 1) > 200 * 1024) {
-      delete e;
-      return fail(GBFFT_ERR_UNSUPPORTED, "axis length " + std::to_string(lens[d]) +
-                                             " does not fit one shared-memory tile at this precision");
-    }
-    e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
-    if (gen_length(lens[d])) e->ax[d].fast_e = gen_points(lens[d]);
-    if (fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
-    if (gen_length(lens[d]) && (tune.e[d] == gen_points(lens[d]) || tune.e[d] == 2))
-      e->ax[d].fast_e = tune.e[d];
-    if (form == GBFFT_FORM_SPLIT && split_length(lens[d])) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
-    int rc = upload_twiddles(e->ax[d], prec);
+    rc = upload_twiddles(e->ax[d], prec);
     if (rc != GBFFT_OK) {
       release(e);
       delete e;
@@ -976,19 +1032,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
     }
     cudaMemset(e->d_sync, 0, (size_t)(nz + 2) * sizeof(int));
   }
-  // tuned tile shapes and fusion for this shape, when the cache has them
-  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
-    if (tune.L[k] > 0 && gbfft_engine_set_tile(e, k, tune.L[k]) != GBFFT_OK) e->tile_L[k] = 0;
-  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
-    if (tune.pipe[k] > 0 && gbfft_engine_set_pipeline(e, k, tune.pipe[k]) != GBFFT_OK) e->pipe[k] = 0;
-  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
-    if (tune.csize[k] > 0 && gbfft_engine_set_cluster(e, k, tune.csize[k], tune.csync[k]) != GBFFT_OK) {
-      e->csize[k] = 0;
-      e->csync[k] = 0;
-    }
-  if (tune.fuse >= 0) e->fuse = tune.fuse != 0;
-  if (tune.pad >= 0 && tune.pad <= 2) e->pad = tune.pad;
-  if (tune.flat >= 0) e->flat = tune.flat != 0;
+  apply_tune(e, tune);
   g_err.clear();
   *engine = e;
   return GBFFT_OK;
@@ -1065,19 +1109,7 @@ int gbfft_exec_c2c(gbfft_engine_t e, void* d_in, void* d_out, int isign, void* s
     return fail(GBFFT_ERR_INVALID, "input and output partially overlap");
   if (!aligned(d_in, cbytes(e)) || !aligned(d_out, cbytes(e)))
     return fail(GBFFT_ERR_INVALID, "array not aligned to its element size");
-  const bool x_first = (e->format == GBFFT_PHYSICAL_IN_X && isign == GBFFT_FORWARD) ||
-                       (e->format == GBFFT_PHYSICAL_IN_Z && isign == GBFFT_BACKWARD);
-  const int order_f[3] = {0, 1, 2}, order_b[3] = {2, 1, 0};
-  const int* order = x_first ? order_f : order_b;
-  const int inv = isign == GBFFT_BACKWARD ? 1 : 0;
-  std::vector<Pass> ps;
-  const void* cur = d_in;
-  for (int i = 0; i < 3; ++i) {
-    const int ax = order[i];
-    if (e->skip[ax]) continue;
-    ps.push_back(c2c_pass(e, ax, n1, n2, n3, cur, d_out, inv, n1, n1));
-    cur = d_out;
-  }
+  std::vector<Pass> ps = c2c_passes(e, d_in, d_out, isign);
   if (ps.empty()) {
     cudaError_t err = launch_copy(d_in, d_out, bytes, st);
     if (err != cudaSuccess) return cuda_fail(err, "copy launch");
@@ -1295,6 +1327,56 @@ int gbfft_engine_get_layout(gbfft_engine_t e, int* pad, int* flat) {
   if (!valid_engine(e) || !pad || !flat) return fail(GBFFT_ERR_INVALID, "bad argument");
   *pad = e->pad;
   *flat = e->flat ? 1 : 0;
+  return GBFFT_OK;
+}
+
+int gbfft_plan_describe(int format, int nx, int ny, int nz, int inplace, const int* skip, int prec, int pad,
+                        int flat, int which, gbfft_pass_desc_t* out, int max_passes, int* n_passes) {
+  if (!n_passes || (max_passes > 0 && !out)) return fail(GBFFT_ERR_INVALID, "null output pointer");
+  *n_passes = 0;
+  int rc = check_engine_args(format, nx, ny, nz, prec, GBFFT_FORM_PLAIN);
+  if (rc != GBFFT_OK) return rc;
+  if (which < 0 || which > 3) return fail(GBFFT_ERR_INVALID, "which must be 0 (r2c), 1 (c2r), 2 or 3 (c2c)");
+  if (pad < -1 || pad > 2) return fail(GBFFT_ERR_INVALID, "pad must be -1, 0, 1 or 2");
+  gbfft_engine_s e;  // no device memory: tables and work area are never touched
+  TuneEntry tune;
+  rc = engine_init_host(&e, format, nx, ny, nz, inplace, skip, prec, GBFFT_FORM_PLAIN, &tune);
+  if (rc != GBFFT_OK) return rc;
+  apply_tune(&e, tune);
+  if (pad >= 0) e.pad = pad;
+  if (flat >= 0) e.flat = flat != 0;
+  // stand-in addresses of the three arrays, never dereferenced (aligned like
+  // device allocations, so that the vector-access choices are the real ones)
+  char* const in = reinterpret_cast<char*>(uintptr_t(1) << 40);
+  char* const outp = in + (uintptr_t(1) << 40);
+  char* const work = outp + (uintptr_t(1) << 40);
+  e.work = e.inplace ? nullptr : work;
+  std::vector<Pass> ps;
+  if (which == 0) ps = r2c_passes(&e, in, outp);
+  else if (which == 1) ps = c2r_passes(&e, in, outp);
+  else ps = c2c_passes(&e, in, outp, which == 2 ? GBFFT_FORWARD : GBFFT_BACKWARD);
+  e.work = nullptr;
+  auto buffer = [&](const void* p) { return p == in ? 0 : p == outp ? 1 : p == work ? 2 : -1; };
+  for (size_t i = 0; i < ps.size() && (int)i < max_passes; ++i) {
+    const PassArgs& a = ps[i].a;
+    gbfft_pass_desc_t& d = out[i];
+    d.kind = ps[i].kind;
+    d.contiguous = ps[i].contiguous ? 1 : 0;
+    d.n = a.n;
+    d.nlines = a.nlines;
+    d.real_lines = a.real_lines;
+    d.nv = a.nv;
+    d.row_w = a.row_w;
+    d.s_src_n = a.s_src_n;
+    d.s_src_l = a.s_src_l;
+    d.s_src_r = a.s_src_r;
+    d.s_dst_n = a.s_dst_n;
+    d.s_dst_l = a.s_dst_l;
+    d.s_dst_r = a.s_dst_r;
+    d.src = buffer(a.src);
+    d.dst = buffer(a.dst);
+  }
+  *n_passes = (int)ps.size();
   return GBFFT_OK;
 }
 

@@ -74,6 +74,7 @@ SIGNATURES = {
     "gbfft_engine_get_cluster": (_i, [_vp, _ip, _ip]),
     "gbfft_engine_set_fusion": (_i, [_vp, _i]),
     "gbfft_engine_set_layout": (_i, [_vp, _i, _i]),
+    "gbfft_plan_describe": (_i, [_i, _i, _i, _i, _i, _ip, _i, _i, _i, _i, _vp, _i, _ip]),
     "gbfft_engine_get_layout": (_i, [_vp, _ip, _ip]),
     "gbfft_engine_status": (_i, [_vp]),
     "gbfft_tune_cache_path": (_i, [ctypes.c_char_p]),
@@ -371,6 +372,28 @@ def transpose(kind, src, dst, n1, n2, n3, is_complex, prec, stream=None):
     check(lib().gbfft_transpose(int(kind), int(bool(is_complex)), int(prec), _ptr(src), _ptr(dst),
                                 int(n1), int(n2), int(n3), _stream(stream)))
     return dst
+
+
+class PassDesc(ctypes.Structure):
+    """gbfft_pass_desc_t: one axis pass of a plan (gbfft_plan_describe)."""
+    _fields_ = [("kind", ctypes.c_int), ("contiguous", ctypes.c_int), ("n", ctypes.c_int),
+                ("row_w", ctypes.c_int), ("nlines", ctypes.c_longlong), ("real_lines", ctypes.c_longlong),
+                ("nv", ctypes.c_longlong), ("s_src_n", ctypes.c_longlong), ("s_src_l", ctypes.c_longlong),
+                ("s_src_r", ctypes.c_longlong), ("s_dst_n", ctypes.c_longlong), ("s_dst_l", ctypes.c_longlong),
+                ("s_dst_r", ctypes.c_longlong), ("src", ctypes.c_int), ("dst", ctypes.c_int)]
+
+
+def plan_describe(fmt, nx, ny, nz, which, inplace=False, skip=(False, False, False), prec=PREC_DOUBLE,
+                  pad=-1, flat=-1):
+    """The axis passes an engine would run (host only, no GPU): which 0 r2c,
+    1 c2r, 2 c2c forward, 3 c2c backward; a list of dicts."""
+    arr = (PassDesc * 8)()
+    n = ctypes.c_int()
+    sk = (ctypes.c_int * 3)(*[int(bool(v)) for v in skip])
+    check(lib().gbfft_plan_describe(int(fmt), int(nx), int(ny), int(nz), int(bool(inplace)), sk, int(prec),
+                                    int(pad), int(flat), int(which), ctypes.cast(arr, ctypes.c_void_p), 8,
+                                    ctypes.byref(n)))
+    return [{f: getattr(arr[i], f) for f, _ in PassDesc._fields_} for i in range(n.value)]
 
 
 class Batch:

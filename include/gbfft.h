@@ -211,6 +211,30 @@ int gbfft_engine_get_cluster(gbfft_engine_t engine, int* ctas, int* sync);
 int gbfft_engine_set_layout(gbfft_engine_t engine, int pad, int flat);
 int gbfft_engine_get_layout(gbfft_engine_t engine, int* pad, int* flat);
 
+/* Host-only description of the axis passes an engine with these arguments
+ * would run (no device memory, no GPU needed): which = 0 r2c, 1 c2r, 2 c2c
+ * forward, 3 c2c backward; pad / flat as gbfft_engine_set_layout, -1 for
+ * the engine's own choice (tuning cache or default).  Fills up to
+ * max_passes entries and sets *n_passes to the number of passes (0 for a
+ * c2c with every axis skipped, which is a copy).  Strides are in elements of
+ * each side's type (real on the real side of r2c / c2r); a pass's lines are
+ * u < nlines (complex lines; real lines u < real_lines for r2c / c2r) and,
+ * on strided axes, v < nv, starting at u * s_l (contiguous), u + v * s_l
+ * (strided) or, when row_w > 0, (u / row_w) * s_r + u % row_w; point n of a
+ * line sits at + n * s_n.  src / dst: 0 the input array, 1 the output
+ * array, 2 the engine's work area.  The x/y fusion is not described. */
+typedef struct {
+  int kind;       /* 0 c2c, 1 r2c, 2 c2r */
+  int contiguous; /* 1: lines along x */
+  int n;          /* points a line (real points for r2c / c2r) */
+  int row_w;
+  long long nlines, real_lines, nv;
+  long long s_src_n, s_src_l, s_src_r, s_dst_n, s_dst_l, s_dst_r;
+  int src, dst;
+} gbfft_pass_desc_t;
+int gbfft_plan_describe(int format, int nx, int ny, int nz, int inplace, const int* skip, int prec, int pad,
+                        int flat, int which, gbfft_pass_desc_t* out, int max_passes, int* n_passes);
+
 /* Pass fusion: 1 (default) lets the engine run the x and y passes of each
  * z-plane in one kernel where a fused kernel exists for the lengths; 0 runs
  * one kernel per axis. */
