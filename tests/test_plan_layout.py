@@ -103,3 +103,44 @@ def test_describe_checks_its_arguments():
         G.plan_describe(1, 8, 8, 8, 4)
     with pytest.raises(G.GbfftError, match="pad"):
         G.plan_describe(1, 8, 8, 8, 0, pad=3)
+
+
+def side_offsets(p, side):
+    """Every element offset a pass touches on one side (numpy array)."""
+    import numpy as np
+    kind, n = p["kind"], p["n"]
+    real_side = (kind == 1 and side == "src") or (kind == 2 and side == "dst")
+    lines = p["nlines"] if kind == 0 else p["real_lines"]
+    pts = n if (kind == 0 or real_side) else n // 2 + 1
+    s_n, s_l, s_r = p["s_" + side + "_n"], p["s_" + side + "_l"], p["s_" + side + "_r"]
+    u = np.arange(lines, dtype=np.int64)
+    if p["contiguous"]:
+        base = u * s_l
+    elif p["row_w"] > 0:
+        base = (u // p["row_w"]) * s_r + u % p["row_w"]
+    else:
+        v = np.arange(p["nv"], dtype=np.int64)
+        base = (u[:, None] + v[None, :] * s_l).ravel()
+    return (base[:, None] + np.arange(pts, dtype=np.int64)[None, :] * s_n).ravel()
+
+
+@pytest.mark.parametrize("fmt", [1, 3])
+@pytest.mark.parametrize("shape", [(34, 12, 10), (33, 17, 9), (64, 16, 8)])
+@pytest.mark.parametrize("pad", [0, 1, 2])
+def test_passes_cover_their_arrays_once(fmt, shape, pad):
+    import numpy as np
+    nx, ny, nz = shape
+    sp = (nx // 2 + 1, ny, nz) if fmt == 1 else (nx, ny, nz // 2 + 1)
+    for which in range(4):
+        for flat in (0, 1):
+            ps = G.plan_describe(fmt, nx, ny, nz, which, prec=4, pad=pad, flat=flat)
+            out_size = {0: sp[0] * sp[1] * sp[2], 1: nx * ny * nz}.get(which, nx * ny * nz)
+            last = side_offsets(ps[-1], "dst")
+            # the last pass writes every element of the output exactly once
+            assert len(last) == out_size and len(np.unique(last)) == out_size, (which, flat)
+            assert last.min() == 0 and last.max() == out_size - 1, (which, flat)
+            # each pass reads exactly the elements the previous one wrote
+            for a, b in zip(ps, ps[1:]):
+                wa = np.unique(side_offsets(a, "dst"))
+                rb = np.unique(side_offsets(b, "src"))
+                assert np.array_equal(wa, rb), (which, flat, a, b)
