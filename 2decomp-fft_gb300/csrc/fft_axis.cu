@@ -103,11 +103,11 @@ template <typename T, int KIND, bool CONTIG>
 cudaError_t launch_typed(const PassArgs& a, cudaStream_t stream) {
   const size_t smem = pass_smem_bytes(sizeof(T), a.n, a.L);
   auto kern = axis_pass_kernel<T, KIND, CONTIG>;
-  static std::atomic<size_t> smem_set{48 * 1024};
-  if (smem > smem_set.load()) {
+  // the limit is a per-device attribute of the kernel: set it on every
+  // launch that needs it (cheap), so a second device is covered too
+  if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    smem_set.store(smem);
   }
   const dim3 block = CONTIG ? dim3(a.tpl, a.L) : dim3(a.L, a.tpl);
   const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);

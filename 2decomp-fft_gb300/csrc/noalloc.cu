@@ -25,7 +25,16 @@
 // first call on each device (with that device current) asks the runtime for
 // the array's device address with cudaGetSymbolAddress and caches it.  Make
 // that first call before any stream capture on that device.
+//
+// When the array is reserved: the CUDA runtime loads a library's device code
+// lazily by default (CUDA_MODULE_LOADING=LAZY), so the 64 MiB are most likely
+// reserved by that first call, not when the library is loaded.  A caller that
+// will reserve all device memory, or enter a region where nothing may
+// allocate, should make one call first (any small grid will do) or run with
+// CUDA_MODULE_LOADING=EAGER.  The cached address belongs to the device's
+// primary context: calling cudaDeviceReset between calls is not supported.
 #include <atomic>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 
@@ -155,6 +164,10 @@ extern "C" int gbfft_exec_c2r_noalloc(int format, int nx, int ny, int nz, int pr
   if (prec != GBFFT_PREC_SINGLE && prec != GBFFT_PREC_DOUBLE)
     return gbfft::set_error(GBFFT_ERR_INVALID, "Invalid value for precision (4 or 8)");
   if (!d_in || !d_out) return gbfft::set_error(GBFFT_ERR_INVALID, "null array pointer");
+  // the kernels load and store whole elements: a complex input aligned to
+  // 2 * prec bytes, a real output to prec bytes (as gbfft_exec_c2r)
+  if ((uintptr_t)d_in % (2 * (uintptr_t)prec) != 0 || (uintptr_t)d_out % (uintptr_t)prec != 0)
+    return gbfft::set_error(GBFFT_ERR_INVALID, "array not aligned to its element size");
   const int lens[3] = {nx, ny, nz};
   Plan plan[3];
   for (int d = 0; d < 3; ++d) {

@@ -286,7 +286,15 @@ int gbfft_engine_profile_read(gbfft_engine_t engine, int kind, long long* launch
  *   - All calls share the array: calls whose GPU work overlaps (other
  *     streams, other host threads) race and corrupt each other.
  *   - The first call on a device (with it current) looks up the array's
- *     device address; make that first call before any stream capture. */
+ *     device address; make that first call before any stream capture.
+ *   - The runtime loads device code lazily by default, so that first call is
+ *     most likely also when the device reserves the array: make it before
+ *     reserving all device memory or entering a region that may not
+ *     allocate, or run with CUDA_MODULE_LOADING=EAGER.
+ *   - The cached address belongs to the primary context: cudaDeviceReset
+ *     between calls is not supported.
+ *   - Arrays must be aligned to their elements, as for gbfft_exec_c2r; a
+ *     misaligned pointer is rejected before any launch. */
 #define GBFFT_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int gbfft_exec_c2r_noalloc(int format, int nx, int ny, int nz, int prec,
                            const void* d_in, void* d_out, void* stream);

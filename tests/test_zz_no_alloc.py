@@ -56,3 +56,21 @@ def test_noalloc_rejects_sizes_beyond_the_static_scratch():
     y = torch.zeros(8, dtype=torch.float64, device="cuda")
     with pytest.raises(gbfft.GbfftError, match="static scratch"):
         gbfft.c2r_noalloc(1, nx, ny, nz, 8, x, y)
+
+
+def test_noalloc_rejects_misaligned_arrays_before_any_launch():
+    """A byte-offset view of a complex or real array is refused with
+    GBFFT_ERR_INVALID on the host (nothing is launched, so nothing faults)."""
+    import ctypes
+
+    import gbfft
+    nx, ny, nz = 16, 8, 4
+    spec = torch.zeros((nz, ny, nx // 2 + 1), dtype=torch.complex128, device="cuda")
+    out = torch.zeros((nz, ny, nx), dtype=torch.float64, device="cuda")
+    before = gbfft.launch_count()
+    lib = gbfft.lib()
+    for din, dout in ((spec.data_ptr() + 8, out.data_ptr()), (spec.data_ptr(), out.data_ptr() + 4)):
+        rc = lib.gbfft_exec_c2r_noalloc(1, nx, ny, nz, 8, ctypes.c_void_p(din), ctypes.c_void_p(dout), None)
+        assert rc == gbfft.ERR_INVALID
+        assert "aligned" in gbfft.last_error()
+    assert gbfft.launch_count() == before
