@@ -15,9 +15,9 @@ sides, max over ranks).  `e2e` is the same metric through the C ABI with
 host buffers: every step copies the input from pinned host memory, runs
 r2c + c2r, and copies the result back.  Inputs (2 GiB real + 2.1 GiB
 spectral) are larger than the 129 MB L2, so no flush is needed between
-steps.  The CPU leg times the oracle -- the restated generic backend of the
-reference -- on a bounded sample of the same line passes and scales it to
-the full grid.
+steps.  The CPU leg times whole round trips of the oracle -- the restated
+generic backend of the reference -- on all host cores, and scipy.fft
+(pocketfft) beside it.
 """
 import argparse
 import json
@@ -206,57 +206,95 @@ def make_input(nx, ny, nz, kind, dtype, device):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle on a bounded sample of the same line passes
+# CPU baseline: whole round trips of the oracle (and of pocketfft) on the host
 # ---------------------------------------------------------------------------
-def cpu_sample(nx, ny, nz, fmt, prec, seconds_target=12.0, threads=None):
-    """Time the generic backend's six line passes of one r2c + c2r round trip
-    on a bounded subset of each pass's lines (the full-size arrays, real
-    strides), and scale each pass to its full line count.  Returns
-    (estimated GPts/s, threads, description)."""
+def host_input(nx, ny, nz, prec, seed=3):
+    """Seeded N(0, 1) host field of the workload's shape; the cost of a line
+    FFT does not depend on the values."""
+    import numpy as np
+    rt = np.float32 if prec == 4 else np.float64
+    return np.random.default_rng(seed).standard_normal((nz, ny, nx), dtype=rt)
+
+
+def cpu_round_trips(x, fmt, prec, steps, warmup, threads=None):
+    """Time whole r2c + c2r round trips of the oracle -- the restated generic
+    backend, every line of all six passes -- as the reference's own test
+    programs time them (examples/fft_physical_x/fft_r2c_x.f90:77-128: one
+    untimed warm-up round trip, then the mean of ntest timed ones).  The
+    arrays are allocated once and the oracle's work arrays persist across
+    calls, as the reference's decomp_pool buffers do.  Returns (seconds per
+    round trip, threads)."""
     import numpy as np
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
     O.set_threads(threads)
     p = "d" if prec == 8 else "s"
-    rt, ct = (np.float64, np.complex128) if prec == 8 else (np.float32, np.complex64)
-    real = np.full((nz, ny, nx), 0.5, dtype=rt)
-    if fmt == 1:
-        s1, s2, s3 = nx // 2 + 1, ny, nz
-        passes = [("r2c", 0, ny * nz), ("c2c", 1, s1 * s3), ("c2c", 2, s1 * s2),
-                  ("c2c", 2, s1 * s2), ("c2c", 1, s1 * s3), ("c2r", 0, ny * nz)]
-    else:
-        s1, s2, s3 = nx, ny, nz // 2 + 1
-        passes = [("r2c", 2, nx * ny), ("c2c", 1, s1 * s3), ("c2c", 0, s2 * s3),
-                  ("c2c", 0, s2 * s3), ("c2c", 1, s1 * s3), ("c2r", 2, nx * ny)]
-    spec = np.full((s3, s2, s1), 0.25 + 0.5j, dtype=ct)
-
-    def run(kind, axis, lines):
-        if kind == "r2c":
-            O.sample_pass("r2c", axis, real, spec, nx, ny, nz, lines, p)
-        elif kind == "c2r":
-            O.sample_pass("c2r", axis, spec, real, nx, ny, nz, lines, p)
-        else:
-            O.sample_pass("c2c", axis, spec, None, s1, s2, s3, lines, p)
-
-    per_pass = seconds_target / len(passes)
-    total_est = 0.0
-    sampled = []
-    for kind, axis, total_lines in passes:
-        probe = min(total_lines, 4 * threads)
+    nz, ny, nx = x.shape
+    ct = np.complex64 if prec == 4 else np.complex128
+    spec = np.empty(O.spectral_shape(nx, ny, nz, fmt), dtype=ct)
+    y = np.empty_like(x)
+    for _ in range(warmup):
+        O.fft3d_r2c_into(x, spec, fmt, p)
+        O.fft3d_c2r_into(spec, y, fmt, p)
+    times = []
+    for _ in range(steps):
         t = time.perf_counter()
-        run(kind, axis, probe)
-        dt = max(time.perf_counter() - t, 1e-6)
-        lines = int(min(total_lines, max(probe, probe * per_pass / dt)))
+        O.fft3d_r2c_into(x, spec, fmt, p)
+        O.fft3d_c2r_into(spec, y, fmt, p)
+        times.append(time.perf_counter() - t)
+    O.pool_release()
+    return sum(times) / len(times), threads
+
+
+def scipy_round_trips(x, fmt, steps, warmup, threads=None):
+    """The FFTW-class CPU stand-in: scipy.fft (pocketfft) rfftn + irfftn in
+    the input's precision with `workers` threads, timed like
+    cpu_round_trips.  Returns (seconds per round trip, threads, version) or
+    None when scipy is missing."""
+    try:
+        import scipy
+        import scipy.fft as sfft
+    except Exception:
+        return None
+    threads = threads or os.cpu_count() or 1
+    nz, ny, nx = x.shape
+    axes = (0, 1, 2) if fmt == 1 else (2, 1, 0)
+    shape = (nz, ny, nx) if fmt == 1 else (nx, ny, nz)
+
+    def rt():
+        s = sfft.rfftn(x, axes=axes, workers=threads)
+        return sfft.irfftn(s, s=shape, axes=axes, workers=threads)
+
+    for _ in range(warmup):
+        rt()
+    times = []
+    for _ in range(steps):
         t = time.perf_counter()
-        run(kind, axis, lines)
-        dt = time.perf_counter() - t
-        total_est += dt * total_lines / lines
-        sampled.append("%s-%s %d/%d lines" % (kind, "xyz"[axis], lines, total_lines))
-    gpts = nx * ny * nz / total_est / 1e9
-    desc = ("oracle (restated generic backend, Glassman FFT, %s) on the first lines of each of the "
-            "6 line passes of one r2c+c2r round trip over the full-size arrays, scaled to all lines: %s"
-            % ("double" if prec == 8 else "single", "; ".join(sampled)))
-    return gpts, threads, desc, total_est
+        rt()
+        times.append(time.perf_counter() - t)
+    return sum(times) / len(times), threads, scipy.__version__
+
+
+def cpu_baseline(nx, ny, nz, fmt, prec, steps=2, warmup=1, x=None):
+    """The cpu_baseline object of the GPU arm's line: the oracle's whole
+    round trips (the value) and scipy.fft's beside it."""
+    x = host_input(nx, ny, nz, prec) if x is None else x
+    npts = nx * ny * nz
+    sec, thr = cpu_round_trips(x, fmt, prec, steps, warmup)
+    out = {"value": round(npts / sec / 1e9, 5), "unit": "GPts/s", "cores": thr, "kind": "port",
+           "ms_per_round_trip": round(sec * 1e3, 1),
+           "sample": "oracle (restated generic backend, Glassman FFT, %s build), OpenMP over lines on %d "
+                     "host threads: whole r2c+c2r round trips of the full grid (every line of all 6 passes), "
+                     "%d untimed warm-up then the mean of %d" % ("double" if prec == 8 else "single", thr,
+                                                                 warmup, steps)}
+    sp = scipy_round_trips(x, fmt, steps, warmup)
+    if sp is not None:
+        out["scipy_fft"] = {"value": round(npts / sp[0] / 1e9, 5), "unit": "GPts/s", "cores": sp[1],
+                            "ms_per_round_trip": round(sp[0] * 1e3, 1),
+                            "sample": "scipy %s scipy.fft.rfftn + irfftn (pocketfft, %s, workers=%d), "
+                                      "%d warm-up then the mean of %d whole round trips"
+                                      % (sp[2], "float32" if prec == 4 else "float64", sp[1], warmup, steps)}
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -478,9 +516,8 @@ def run_gb300(args):
                    "fp64_reference": "pocketfft (scipy.fft) FP64 on the same input"}
         cpu = None
         if not args.no_cpu:
-            g, thr, desc, est = cpu_sample(nx, ny, nz, fmt, prec, seconds_target=args.cpu_seconds)
-            cpu = {"value": round(g, 5), "unit": "GPts/s", "cores": thr, "kind": "port",
-                   "sample": desc, "est_seconds_full_round_trip": round(est, 2)}
+            cpu = cpu_baseline(nx, ny, nz, fmt, prec, steps=args.cpu_steps, warmup=1,
+                               x=x.cpu().numpy())
         out = {
             "metric": METRIC,
             "value": round(value, 3),
@@ -783,6 +820,11 @@ def run_dtt(args):
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU path for this workload -- the
+    oracle, a restatement of its generic backend (the Fortran reference
+    cannot be built on these machines) -- on all host cores.  Every step is
+    one whole r2c + c2r round trip of the full grid; W untimed steps, then
+    the mean of K timed ones."""
     world, rank, local = dist_env()
     if rank != 0:
         return None
@@ -791,26 +833,26 @@ def run_reference(args):
                           "%s has no CPU reference run" % args.workload}), flush=True)
         return None
     nx, ny, nz, fmt, prec, kind = WORKLOADS[args.workload]
-    threads = os.cpu_count() or 1
-    per_step = max(1.0, args.ref_step_seconds)
-    vals = []
-    desc = ""
-    for i in range(args.warmup + args.steps):
-        g, thr, desc, est = cpu_sample(nx, ny, nz, fmt, prec, seconds_target=per_step, threads=threads)
-        if i >= args.warmup:
-            vals.append(g)
-    v = sum(vals) / len(vals)
+    x = host_input(nx, ny, nz, prec)
+    t0 = time.time()
+    sec, threads = cpu_round_trips(x, fmt, prec, args.steps, args.warmup)
+    wall = time.time() - t0
+    v = nx * ny * nz / sec / 1e9
+    desc = ("oracle (restated generic backend, Glassman FFT, %s build), OpenMP over lines on %d host threads: "
+            "each step one whole r2c+c2r round trip of the full grid (every line of all 6 passes)"
+            % ("double" if prec == 8 else "single", threads))
     out = {"metric": METRIC, "value": round(v, 5), "unit": "GPts/s", "n_gpus": world,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(nx * ny * nz / (v * 1e9) * 1e3, 3),
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f32" if prec == 4 else "f64", "data": "synthetic (constant-valued arrays; the "
-           "line FFT cost does not depend on the values)", "impl": "reference",
+           "dtype": "f32" if prec == 4 else "f64", "data": "synthetic: seeded N(0,1) host field (the line FFT "
+           "cost does not depend on the values)", "impl": "reference",
            "config": {"workload": "r2c+c2r round trip %dx%dx%d %s %s" % (
                nx, ny, nz, "fp32" if prec == 4 else "fp64", "PHYSICAL_IN_X" if fmt == 1 else "PHYSICAL_IN_Z"),
                "name": args.workload, "nx": nx, "ny": ny, "nz": nz,
                "parallelism": "OpenMP threads over lines on the host cores"},
            "cpu_baseline": {"value": round(v, 5), "unit": "GPts/s", "cores": threads, "kind": "port",
                             "sample": desc},
+           "timed_wall_s": round(wall, 2),
            "e2e": {"value": round(v, 5), "unit": "GPts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     return out
@@ -828,8 +870,10 @@ def main():
                     help="plain FP32/FP64 stages, or split-FP16 tensor-core radix-16 stages (FP32 only)")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--ref-step-seconds", type=float, default=3.0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="CPU time budget of the r2r workloads' oracle leg")
+    ap.add_argument("--cpu-steps", type=int, default=2,
+                    help="timed whole round trips of the CPU leg (after one warm-up)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -43,6 +43,52 @@
 #define FFT_FORWARD (-1)
 #define FFT_BACKWARD 1
 
+/* Work arrays of the 3D drivers come from a pool that persists across calls,
+ * as the reference's decomp_pool_get buffers do (src/fft_common_3d.f90:209-230),
+ * so that a timed round trip does not pay for fresh pages.  Slot 0: the
+ * input-preserving copy (wk1), slot 1: wk2_r2c.  Not thread-safe: one host
+ * thread calls the oracle at a time (OpenMP works inside the calls). */
+static void* g_pool[2];
+static size_t g_pool_bytes[2];
+
+static void* pool_get(int slot, size_t bytes) {
+  if (g_pool_bytes[slot] < bytes) {
+    free(g_pool[slot]);
+    g_pool[slot] = malloc(bytes);
+    g_pool_bytes[slot] = g_pool[slot] ? bytes : 0;
+  }
+  return g_pool[slot];
+}
+
+int oracle_pool_release(void) {
+  for (int i = 0; i < 2; ++i) {
+    free(g_pool[i]);
+    g_pool[i] = NULL;
+    g_pool_bytes[i] = 0;
+  }
+  return 0;
+}
+
+/* Copy of whole arrays split over the OpenMP threads: at P ranks each rank
+ * copies its own pencil, so the P-thread stand-in copies in parallel too. */
+static void par_copy(void* dst, const void* src, size_t bytes) {
+  if (dst == src) return;
+  const char* s = (const char*)src;
+  char* d = (char*)dst;
+  if ((d < s + bytes) && (s < d + bytes)) {
+    memmove(dst, src, bytes);
+    return;
+  }
+  const size_t chunk = (size_t)1 << 20;
+  long nch = (long)((bytes + chunk - 1) / chunk);
+  _Pragma("omp parallel for schedule(static)")
+  for (long c = 0; c < nch; ++c) {
+    size_t o = (size_t)c * chunk;
+    size_t len = bytes - o < chunk ? bytes - o : chunk;
+    memcpy(d + o, s + o, len);
+  }
+}
+
 #define DEFINE_ORACLE(T, SFX)                                                           \
   typedef struct { T re, im; } cplx_##SFX;                                              \
                                                                                         \
@@ -208,7 +254,7 @@
   }                                                                                     \
                                                                                         \
   static void copy_##SFX(void* dst, const void* src, size_t bytes) {                    \
-    if (dst != src) memmove(dst, src, bytes);                                           \
+    par_copy(dst, src, bytes);                                                          \
   }                                                                                     \
                                                                                         \
   /* src/fft_common_3d.f90:9-116 at dims = (1,1).  `in` is modified when        */     \
@@ -223,9 +269,9 @@
     int fwd_x = (format == PHYSICAL_IN_X && isign == FFT_FORWARD) ||                    \
                 (format == PHYSICAL_IN_Z && isign == FFT_BACKWARD);                     \
     if (!inplace) {                                                                     \
-      wk = (cplx_##SFX*)malloc(bytes);                                                  \
+      wk = (cplx_##SFX*)pool_get(0, bytes);                                             \
       if (!wk) return 1;                                                                \
-      memcpy(wk, in, bytes);                                                            \
+      par_copy(wk, in, bytes);                                                          \
     }                                                                                   \
     if (fwd_x) {                                                                        \
       if (!sx) c2c_lines_##SFX(wk, nx, ny, nz, 0, isign, -1);                               \
@@ -238,7 +284,6 @@
       if (!sy) c2c_lines_##SFX(out, nx, ny, nz, 1, isign, -1);                              \
       if (!sx) c2c_lines_##SFX(out, nx, ny, nz, 0, isign, -1);                              \
     }                                                                                   \
-    if (!inplace) free(wk);                                                             \
     return 0;                                                                           \
   }                                                                                     \
                                                                                         \
@@ -276,26 +321,24 @@
     cplx_##SFX* wk = in;                                                                \
     cplx_##SFX* wk2;                                                                    \
     if (format != PHYSICAL_IN_X && format != PHYSICAL_IN_Z) return 2;                   \
-    wk2 = (cplx_##SFX*)malloc(bytes);                                                   \
+    wk2 = (cplx_##SFX*)pool_get(1, bytes);                                              \
     if (!wk2) return 1;                                                                 \
     if (!inplace) {                                                                     \
-      wk = (cplx_##SFX*)malloc(bytes);                                                  \
-      if (!wk) { free(wk2); return 1; }                                                 \
-      memcpy(wk, in, bytes);                                                            \
+      wk = (cplx_##SFX*)pool_get(0, bytes);                                             \
+      if (!wk) return 1;                                                                \
+      par_copy(wk, in, bytes);                                                          \
     }                                                                                   \
     if (format == PHYSICAL_IN_X) {                                                      \
       if (!sz) c2c_lines_##SFX(wk, s1, ny, s3, 2, FFT_BACKWARD, -1);                        \
-      memcpy(wk2, wk, bytes); /* transpose_z_to_y */                                   \
+      par_copy(wk2, wk, bytes); /* transpose_z_to_y */                                 \
       if (!sy) c2c_lines_##SFX(wk2, s1, ny, s3, 1, FFT_BACKWARD, -1);                       \
       c2r_lines_##SFX(wk2, out, nx, ny, nz, 0, -1);                                         \
     } else {                                                                            \
       if (!sx) c2c_lines_##SFX(wk, s1, ny, s3, 0, FFT_BACKWARD, -1);                        \
       if (!sy) c2c_lines_##SFX(wk, s1, ny, s3, 1, FFT_BACKWARD, -1);                        \
-      memcpy(wk2, wk, bytes); /* transpose_y_to_z into wk13 */                         \
+      par_copy(wk2, wk, bytes); /* transpose_y_to_z into wk13 */                       \
       c2r_lines_##SFX(wk2, out, nx, ny, nz, 2, -1);                                         \
     }                                                                                   \
-    free(wk2);                                                                          \
-    if (!inplace) free(wk);                                                             \
     return 0;                                                                           \
   }
 

@@ -44,6 +44,7 @@ def lib():
             getattr(L, "oracle_fft3d_c2r_" + sfx).argtypes = [vp, vp, ip, ip, ip, ip, ip, vp]
             getattr(L, "oracle_sample_" + sfx).argtypes = [ip, ip, vp, vp, ip, ip, ip, ctypes.c_long]
         L.oracle_transpose_copy.argtypes = [vp, vp, ctypes.c_size_t]
+        L.oracle_pool_release.argtypes = []
         L.oracle_set_threads.argtypes = [ip]
         L.oracle_set_threads.restype = ip
         _lib = L
@@ -133,6 +134,39 @@ def fft3d_c2r(c, nx, ny, nz, fmt, inplace=False, skip=None, prec="d"):
         c.ctypes.data, out.ctypes.data, nx, ny, nz, int(fmt), int(bool(inplace)), sp)
     _check(rc, "fft3d_c2r")
     return out
+
+
+def fft3d_r2c_into(a, out, fmt, prec="d"):
+    """fft3d_r2c writing into a preallocated spectral array ``out`` (for
+    timing: nothing is allocated per call)."""
+    sfx, rt, ct = _types(prec)
+    nz, ny, nx = a.shape
+    if (a.dtype != rt or out.dtype != ct or not a.flags.c_contiguous or not out.flags.c_contiguous
+            or out.shape != spectral_shape(nx, ny, nz, fmt)):
+        raise TypeError("r2c_into: contiguous %s input and %s spectral output required"
+                        % (np.dtype(rt), np.dtype(ct)))
+    _check(getattr(lib(), "oracle_fft3d_r2c_" + sfx)(a.ctypes.data, out.ctypes.data, nx, ny, nz, int(fmt),
+                                                      None), "fft3d_r2c")
+    return out
+
+
+def fft3d_c2r_into(c, out, fmt, prec="d"):
+    """fft3d_c2r (input preserved) writing into a preallocated real array."""
+    sfx, rt, ct = _types(prec)
+    nz, ny, nx = out.shape
+    if (c.dtype != ct or out.dtype != rt or not c.flags.c_contiguous or not out.flags.c_contiguous
+            or c.shape != spectral_shape(nx, ny, nz, fmt)):
+        raise TypeError("c2r_into: contiguous %s spectral input and %s output required"
+                        % (np.dtype(ct), np.dtype(rt)))
+    _check(getattr(lib(), "oracle_fft3d_c2r_" + sfx)(c.ctypes.data, out.ctypes.data, nx, ny, nz, int(fmt), 0,
+                                                      None), "fft3d_c2r")
+    return out
+
+
+def pool_release():
+    """Free the oracle's persistent work arrays (the stand-in for the
+    reference's decomp_pool)."""
+    lib().oracle_pool_release()
 
 
 def transpose(src):
