@@ -200,11 +200,11 @@ struct TuneEntry {
   int prec = 0, format = 0, nx = 0, ny = 0, nz = 0;
   int fuse = -1;
   int L[GBFFT_PASS_KINDS] = {0};
-  int pipe[GBFFT_PASS_KINDS] = {0};
   int csize[GBFFT_PASS_KINDS] = {0};
   int csync[GBFFT_PASS_KINDS] = {0};
   int e[3] = {0, 0, 0};
   int pad = -1, flat = -1;
+  int tma = -1;
 };
 
 std::mutex g_tune_mu;
@@ -253,9 +253,9 @@ void load_tune_locked() {
       else if (k == "e_z") t.e[2] = v;
       else if (k == "pad") t.pad = v;
       else if (k == "flat") t.flat = v;
+      else if (k == "tma") t.tma = v;
       for (int i = 0; i < GBFFT_PASS_KINDS; ++i) {
         if (k == names[i]) t.L[i] = v;
-        if (k == std::string("pipe_") + names[i]) t.pipe[i] = v;
         if (k == std::string("cl_") + names[i]) t.csize[i] = v;
         if (k == std::string("cls_") + names[i]) t.csync[i] = v;
       }
@@ -297,7 +297,6 @@ struct gbfft_engine_s {
   int sp[3] = {0, 0, 0};
   AxisPlan ax[3];
   int tile_L[GBFFT_PASS_KINDS] = {0};  // tuned lines per CTA, 0 = built-in
-  int pipe[GBFFT_PASS_KINDS] = {0};    // tile buffers of the pipelined kernel, 0 = one-shot
   int csize[GBFFT_PASS_KINDS] = {0};   // cluster launch of the one-shot kernel, 0 = none
   int csync[GBFFT_PASS_KINDS] = {0};   // with it, a cluster barrier at the start
   bool fuse = false;                   // fuse x/y passes per plane when possible
@@ -314,6 +313,10 @@ struct gbfft_engine_s {
   // (segments aligned as the plane is).
   int pad = 0;
   bool flat = true;
+  // strided FP32 c2c passes of 256, 512 and 1024 points whose source rows
+  // allow it run the persistent kernel fed by bulk tensor copies
+  bool tma = true;
+  int* d_status = nullptr;  // set to 1 by a bounded wait that gave up
 };
 
 namespace {
@@ -340,6 +343,8 @@ void release(gbfft_engine_t e) {
   e->work = nullptr;
   if (e->d_sync) cudaFree(e->d_sync);
   e->d_sync = nullptr;
+  if (e->d_status) cudaFree(e->d_status);
+  e->d_status = nullptr;
 }
 
 size_t cbytes(const gbfft_engine_s* e) { return 2 * (size_t)e->prec; }
@@ -463,7 +468,7 @@ int gen_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int fo
 }
 
 void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind, int forced_L,
-               bool split = false, int pipe = 0, int csize = 0, int csync = 0) {
+               bool split = false, int csize = 0, int csync = 0) {
   if (split && split_length(p.n)) {
     a.n = p.n;
     a.nst = 0;
@@ -509,28 +514,8 @@ void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int ki
     a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L, fe);
     a.first_fused = 1;
     a.last_fused = kind != K_R2C;
-    a.pipe = 0;
     a.csize = csize > 1 ? csize : 0;
     a.csync = a.csize ? csync : 0;
-    // (the pipelined kernel's copy loop addresses lines as (u, v) only)
-    if (pipe > 0 && prec == 4 && pipe_length(p.n) && a.row_w == 0) {
-      // power-of-two tile heights only (the copy loop indexes by shifts),
-      // and every buffer of the CTA within the shared-memory limit
-      int L = 1;
-      while (2 * L <= a.L) L *= 2;
-      if (contiguous && forced_L <= 0) {
-        L = 1;
-        while (2 * L * a.tpl <= 256) L *= 2;
-      }
-      while (L > 1 && L * a.tpl > pipe_max_threads(fe)) L /= 2;
-      while (L > 1 && (size_t)pipe * fast_smem_entries(p.n, L) * sizeof(float2) > kPipeSmemLimit) L /= 2;
-      if ((size_t)pipe * fast_smem_entries(p.n, L) * sizeof(float2) <= kPipeSmemLimit) {
-        a.L = L;
-        a.pipe = pipe;
-        a.csize = 0;
-        a.csync = 0;
-      }
-    }
     return;
   }
   a.n = p.n;
@@ -599,8 +584,17 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
     }
   }
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C, e->tile_L[GBFFT_PASS_C2C_X + axis],
-            e->form == GBFFT_FORM_SPLIT, e->pipe[GBFFT_PASS_C2C_X + axis], e->csize[GBFFT_PASS_C2C_X + axis],
+            e->form == GBFFT_FORM_SPLIT, e->csize[GBFFT_PASS_C2C_X + axis],
             e->csync[GBFFT_PASS_C2C_X + axis]);
+  // strided power-of-two FP32 passes over rows a tensor map can describe:
+  // the persistent kernel whose tiles arrive by bulk tensor copies (its plan
+  // shares the axis's stage-major twiddle table)
+  if (e->tma && e->d_status && a.fast == 1 && tma_pass_supported(e->prec, K_C2C, P.contiguous, a)) {
+    a.tma = 1;
+    a.status = e->d_status;
+    a.csize = 0;
+    a.csync = 0;
+  }
   P.prof_kind = GBFFT_PASS_C2C_X + axis;
   P.bytes = 2.0 * (double)n1 * n2 * n3 * (double)cbytes(e);
   return P;
@@ -672,7 +666,6 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst, lo
   const int axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, kind,
             e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R], e->form == GBFFT_FORM_SPLIT,
-            e->pipe[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R],
             e->csize[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R],
             e->csync[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R]);
   P.prof_kind = kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R;
@@ -700,7 +693,8 @@ void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
     Pass& py = xfirst ? p1 : p0;
     if (p1.a.src != p0.a.dst) continue;
     if (!fast_length(px.a.n) || !fast_length(py.a.n)) continue;
-    if (px.a.fast != 1 || py.a.fast != 1 || px.a.pipe || py.a.pipe || px.a.csize || py.a.csize) continue;
+    if (px.a.fast != 1 || py.a.fast != 1 || px.a.csize || py.a.csize) continue;
+    if (px.a.tma || py.a.tma) continue;
     if (e->ax[1].fast_e != fast_points(py.a.n, false)) continue;  // the fused kernel's y plan
     if (e->ax[0].fast_e != fast_points(px.a.n, true)) continue;   // and its x plan
     if (!fused_supported(e->prec, px.kind, xfirst, px.a.n, py.a.n)) continue;
@@ -739,7 +733,7 @@ void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
 
 int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st) {
   for (const Pass& p : ps) {
-    if (!p.contiguous && p.a.nv > 65535)
+    if (!p.contiguous && p.a.nv > 65535 && !p.a.tma)
       return fail(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
     ProfRec rec{p.prof_kind, nullptr, nullptr, p.bytes};
     if (e->profiling) {
@@ -844,8 +838,6 @@ void apply_tune(gbfft_engine_s* e, const TuneEntry& tune) {
   for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
     if (tune.L[k] > 0 && gbfft_engine_set_tile(e, k, tune.L[k]) != GBFFT_OK) e->tile_L[k] = 0;
   for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
-    if (tune.pipe[k] > 0 && gbfft_engine_set_pipeline(e, k, tune.pipe[k]) != GBFFT_OK) e->pipe[k] = 0;
-  for (int k = 0; k < GBFFT_PASS_KINDS; ++k)
     if (tune.csize[k] > 0 && gbfft_engine_set_cluster(e, k, tune.csize[k], tune.csync[k]) != GBFFT_OK) {
       e->csize[k] = 0;
       e->csync[k] = 0;
@@ -853,6 +845,7 @@ void apply_tune(gbfft_engine_s* e, const TuneEntry& tune) {
   if (tune.fuse >= 0) e->fuse = tune.fuse != 0;
   if (tune.pad >= 0 && tune.pad <= 2) e->pad = tune.pad;
   if (tune.flat >= 0) e->flat = tune.flat != 0;
+  if (tune.tma >= 0) e->tma = tune.tma != 0;
 }
 
 // The passes of a 3D c2c (src/fft_common_3d.f90:9-116): x, y, z (forward
@@ -964,6 +957,8 @@ int gbfft_version(int* major, int* minor) {
 
 long long gbfft_launch_count(void) { return launch_counter(); }
 
+long long gbfft_tma_pass_count(void) { return tma_launch_counter(); }
+
 int gbfft_malloc(void** d_ptr, size_t bytes) {
   if (!d_ptr) return fail(GBFFT_ERR_INVALID, "gbfft_malloc: null output pointer");
   *d_ptr = nullptr;
@@ -1031,6 +1026,17 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
       return GBFFT_ERR_ALLOC;
     }
     cudaMemset(e->d_sync, 0, (size_t)(nz + 2) * sizeof(int));
+  }
+  {
+    cudaError_t err = cudaMalloc(&e->d_status, 4 * sizeof(int));
+    if (err != cudaSuccess) {
+      e->d_status = nullptr;
+      release(e);
+      delete e;
+      g_err = std::string("cudaMalloc(status word): ") + cudaGetErrorString(err);
+      return GBFFT_ERR_ALLOC;
+    }
+    cudaMemset(e->d_status, 0, 4 * sizeof(int));
   }
   apply_tune(e, tune);
   g_err.clear();
@@ -1208,14 +1214,6 @@ int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
   return GBFFT_OK;
 }
 
-int gbfft_engine_set_pipeline(gbfft_engine_t e, int kind, int depth) {
-  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
-  if (kind < 0 || kind >= GBFFT_PASS_KINDS) return fail(GBFFT_ERR_INVALID, "bad pass kind");
-  if (depth != 0 && depth != 2 && depth != 3) return fail(GBFFT_ERR_INVALID, "pipeline depth must be 0, 2 or 3");
-  e->pipe[kind] = depth;
-  return GBFFT_OK;
-}
-
 int gbfft_engine_set_cluster(gbfft_engine_t e, int kind, int ctas, int sync) {
   if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
   if (kind < 0 || kind >= GBFFT_PASS_KINDS) return fail(GBFFT_ERR_INVALID, "bad pass kind");
@@ -1235,19 +1233,30 @@ int gbfft_engine_get_cluster(gbfft_engine_t e, int* ctas, int* sync) {
   return GBFFT_OK;
 }
 
-int gbfft_engine_get_pipeline(gbfft_engine_t e, int* depth) {
-  if (!valid_engine(e) || !depth) return fail(GBFFT_ERR_INVALID, "bad argument");
-  for (int k = 0; k < GBFFT_PASS_KINDS; ++k) depth[k] = e->pipe[k];
-  return GBFFT_OK;
-}
-
 int gbfft_engine_status(gbfft_engine_t e) {
   if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
-  if (!e->d_sync) return GBFFT_OK;
   int flag = 0;
+  if (e->d_status) {
+    cudaError_t err = cudaMemcpy(&flag, e->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaMemcpy(status)");
+    if (flag) return fail(GBFFT_ERR_TIMEOUT, "a pass gave up waiting for its bulk tensor copies");
+  }
+  if (!e->d_sync) return GBFFT_OK;
   cudaError_t err = cudaMemcpy(&flag, e->d_sync + 1, sizeof(int), cudaMemcpyDeviceToHost);
   if (err != cudaSuccess) return cuda_fail(err, "cudaMemcpy(status)");
   if (flag) return fail(GBFFT_ERR_TIMEOUT, "a fused pass gave up waiting for its plane");
+  return GBFFT_OK;
+}
+
+int gbfft_engine_set_tma(gbfft_engine_t e, int enable) {
+  if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
+  e->tma = enable != 0;
+  return GBFFT_OK;
+}
+
+int gbfft_engine_get_tma(gbfft_engine_t e, int* enable) {
+  if (!valid_engine(e) || !enable) return fail(GBFFT_ERR_INVALID, "bad argument");
+  *enable = e->tma ? 1 : 0;
   return GBFFT_OK;
 }
 

@@ -157,9 +157,9 @@ size_t pass_smem_bytes(int prec_bytes, int n, int L) {
 
 cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a,
                              cudaStream_t stream) {
-  if (a.fast == 1 && a.pipe) {
-    if (prec_bytes != 4) return cudaErrorInvalidValue;
-    return launch_pipe_f32(kind, contiguous, a, stream);
+  if (a.tma) {
+    if (!tma_pass_supported(prec_bytes, kind, contiguous, a)) return cudaErrorInvalidValue;
+    return launch_tma_pass(a, stream);
   }
   if (a.fast == 4) return prec_bytes == 4 ? launch_gen_f32(kind, contiguous, a, stream)
                                           : launch_gen_f64(kind, contiguous, a, stream);

@@ -63,8 +63,6 @@ struct PassArgs {
                    // pair are adjacent and aligned (read/write as one pair);
                    // bit 1 (FP32): so are their two complex lines, 16-byte
                    // aligned (one 16-byte access for both)
-  int pipe;        // fast == 1: 0 = one-shot kernel, 2 or 3 = pipelined
-                   // persistent kernel with that many tile buffers
   int csize;       // fast == 1, one-shot: 0, or launch CTAs in clusters of
                    // csize neighbours (co-scheduled: their row segments
                    // reach DRAM together)
@@ -76,6 +74,11 @@ struct PassArgs {
                    // u % row_w + (u / row_w) * s_src_r (s_dst_r), so that
                    // a tile's row segments are as aligned as the plane
   long long s_src_r, s_dst_r;
+  int tma;         // strided FP32 c2c pass (fast == 1) run by the persistent
+                   // kernel whose tiles arrive by bulk tensor copies
+                   // (fft_tma.cu); needs tma_pass_supported()
+  int* status;     // device word set to 1 when a bounded wait of the pass
+                   // gave up (null: not recorded)
   int radix[kMaxStages];
 };
 
@@ -147,20 +150,12 @@ cudaError_t launch_gen_f64(int kind, bool contiguous, const PassArgs& a, cudaStr
 bool split_length(int n);
 int split_lines_per_cta(int n, bool contiguous);
 cudaError_t launch_split_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
-// Pipelined persistent passes (fft_pipe.cuh): FP32 lines of 256, 512, 1024
-// points; all tile buffers of a CTA within kPipeSmemLimit bytes.
-constexpr size_t kPipeSmemLimit = 226 * 1024;
-bool pipe_length(int n);
-cudaError_t launch_pipe_f32(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 cudaError_t launch_mixed_f64(int kind, bool contiguous, const PassArgs& a, cudaStream_t s);
 
 // Thread limit of the power-of-two kernel for E points a thread.
 __host__ __device__ constexpr int fast_max_threads(int e, int prec_bytes) {
   return e == 32 ? (prec_bytes == 4 ? 512 : 256) : (prec_bytes == 4 ? kFastMaxThreadsF32 : kFastMaxThreadsF64);
 }
-// Thread limit of the pipelined kernel (one CTA per SM, registers for E
-// points plus the copy loop's addressing).
-__host__ __device__ constexpr int pipe_max_threads(int e) { return e == 32 ? 256 : 512; }
 // Shared-memory entries of one power-of-two tile of L lines: the exchange
 // buffer, or for c2r the staged half spectra (n/2+1 per real line).
 __host__ __device__ constexpr long long fast_smem_entries(int n, int L) {
@@ -262,6 +257,15 @@ __host__ __device__ constexpr bool dtt_fast_length(int M) { return M >= 32 && M 
 // runtime plan).
 __host__ __device__ constexpr bool dtt_mixed_length(int M) { return M == 126 || M == 510; }
 cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream);
+
+// TMA-staged strided c2c passes (fft_tma.cu): FP32 lines of 256, 512 or
+// 1024 points whose source rows and planes lie multiples of 16 bytes apart
+// and start 16-byte aligned, on the axis's own compile-time plan (a.tpl =
+// n / 16, or n / 32 for 512 and 1024 points; the stage-major twiddle table
+// is the axis's).
+bool tma_pass_supported(int prec_bytes, int kind, bool contiguous, const PassArgs& a);
+cudaError_t launch_tma_pass(const PassArgs& a, cudaStream_t stream);
+long long tma_launch_counter();
 
 // Enqueue one axis pass.  prec_bytes = 4 (float) or 8 (double).
 cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous,

@@ -64,8 +64,6 @@ SIGNATURES = {
     "gbfft_batch_destroy": (_i, [_vp]),
     "gbfft_engine_set_profiling": (_i, [_vp, _i]),
     "gbfft_engine_set_tile": (_i, [_vp, _i, _i]),
-    "gbfft_engine_set_pipeline": (_i, [_vp, _i, _i]),
-    "gbfft_engine_get_pipeline": (_i, [_vp, _ip]),
     "gbfft_engine_set_cluster": (_i, [_vp, _i, _i, _i]),
     "gbfft_dtt_create": (_i, [_i, _i, _i, _i, _ip, _i, _ip, _i, ctypes.POINTER(_vp)]),
     "gbfft_dtt_destroy": (_i, [_vp]),
@@ -86,6 +84,9 @@ SIGNATURES = {
     "gbfft_selftest_bounded_wait": (_i, [_i, _i, ctypes.c_longlong, _ip]),
     "gbfft_version": (_i, [_ip, _ip]),
     "gbfft_launch_count": (ctypes.c_longlong, []),
+    "gbfft_tma_pass_count": (ctypes.c_longlong, []),
+    "gbfft_engine_set_tma": (_i, [_vp, _i]),
+    "gbfft_engine_get_tma": (_i, [_vp, _ip]),
     # decomp_2d_fft.h
     "d2d_decomp_2d_init": (_i, [_i, _i, _i, _i, _i, _i]),
     "d2d_decomp_2d_finalize": (_i, []),
@@ -159,6 +160,11 @@ def check(status):
 
 def launch_count():
     return int(lib().gbfft_launch_count())
+
+
+def tma_pass_count():
+    """Strided passes run so far by the bulk-tensor-copy kernel."""
+    return int(lib().gbfft_tma_pass_count())
 
 
 def _ptr(t):
@@ -270,12 +276,6 @@ class Engine:
         check(lib().gbfft_engine_set_tile(self.h, int(kind), int(lines)))
 
 
-    def set_pipeline(self, kind, depth):
-        """Pipelined persistent kernel for a pass kind (name or GBFFT_PASS_*):
-        depth 2 or 3 tile buffers, 0 = one CTA per tile."""
-        k = PASS_NAMES.index(kind) if isinstance(kind, str) else int(kind)
-        check(lib().gbfft_engine_set_pipeline(self.h, k, int(depth)))
-
     def set_cluster(self, kind, ctas, sync=True):
         """Launch a pass kind's CTAs in clusters of ctas (2, 4, 8; 0 = off),
         with a cluster barrier at the start when sync."""
@@ -287,10 +287,15 @@ class Engine:
         check(lib().gbfft_engine_get_cluster(self.h, c, s))
         return {k: (c[i], s[i]) for i, k in enumerate(PASS_NAMES)}
 
-    def pipeline(self):
-        d = (ctypes.c_int * len(PASS_NAMES))()
-        check(lib().gbfft_engine_get_pipeline(self.h, d))
-        return dict(zip(PASS_NAMES, d))
+    def set_tma(self, enable):
+        """Run eligible strided passes with the bulk-tensor-copy kernel."""
+        check(lib().gbfft_engine_set_tma(self.h, int(bool(enable))))
+
+    def tma(self):
+        v = ctypes.c_int(0)
+        check(lib().gbfft_engine_get_tma(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
     def set_layout(self, pad=1, flat=True):
         """Padded work-area rows (aligned row segments for the strided passes):
         pad 1 (or True) for r2c and c2r, 2 for c2r only, 0 (default) none;

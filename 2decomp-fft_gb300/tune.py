@@ -8,20 +8,23 @@ creation (tune_cache.txt beside this file, or $GBFFT_TUNE_CACHE):
     (radix 16 stages) or 32 (two radix-32 stages); of axes of 243, 270,
     360, 384, 400 points: the balanced plan or the two-stage one (2)
                                                                -> e_x, e_y, e_z
+  * row layout: padded work-area rows, flat z passes          -> pad, flat
+  * strided passes staged by bulk tensor copies or one-shot    -> tma
   * the tile shape (lines per CTA) of every pass kind          -> r2c, c2r,
                                                                   c2c_x, c2c_y,
                                                                   c2c_z, xy_fused
-  * launch form: one CTA per tile, the same in clusters of 2, 4 or 8
-    neighbouring CTAs (with or without a start barrier), or a
-    persistent kernel streaming tiles through 2 or 3 shared-memory
-    buffers                                                    -> cl_<pass>,
-                                                                  cls_<pass>,
-                                                                  pipe_<pass>
-  * row layout: padded work-area rows, flat z passes          -> pad, flat
+  * launch form of the one-shot kernels: one CTA per tile, or clusters of
+    2, 4 or 8 neighbouring CTAs (with or without a start barrier)
+                                                               -> cl_<pass>,
+                                                                  cls_<pass>
   * pass fusion: x and y passes of each z-plane in one kernel  -> fuse
 
-The measured step is the benchmark's: one r2c then one c2r, per-pass device
-times from CUDA events on the launching stream.
+Plans, layouts and the staging choice interact (the bulk-copy kernel needs
+rows a tensor map can describe, and shares the axis plan's twiddles), so
+every combination of the three is timed first; tile shapes and launch forms
+are then tuned pass by pass for the fastest.  The measured step is the
+benchmark's: one r2c then one c2r, per-pass device times from CUDA events on
+the launching stream.
 
     python tune.py [--out FILE] [--shapes prec,fmt,nx,ny,nz ...]
 """
@@ -45,9 +48,9 @@ DEFAULT_SHAPES = [
 ]
 TILES = [1, 2, 4, 8, 16, 32]
 MARGIN = 0.99
-# launch forms: (pipeline depth, (cluster CTAs, start barrier)); one-shot
-# kernels plain or in clusters, or the pipelined kernel with 2 or 3 buffers
-LAUNCHES = [(0, (0, 0)), (0, (2, 0)), (0, (2, 1)), (0, (4, 1)), (0, (8, 1)), (2, (0, 0)), (3, (0, 0))]
+# launch forms of the one-shot kernels: (cluster CTAs, start barrier)
+LAUNCHES = [(0, 0), (2, 0), (2, 1), (4, 1), (8, 1)]
+LAYOUTS = [(0, True), (1, True), (2, True), (0, False), (1, False)]
 
 
 def measure(eng, x, s, y, steps=6, warm=2):
@@ -87,82 +90,65 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     for axis, n in ((0, nx), (1, ny), (2, nz)):
         opts[axis] = [16, 32] if n in (512, 1024) else ([balanced[n], 2] if n in balanced else [None])
     eng.set_fusion(False)
+
+    def apply(ex, ey, ez, layout, tma):
+        for axis, pts in ((0, ex), (1, ey), (2, ez)):
+            if pts:
+                eng.set_plan(axis, pts)
+        eng.set_layout(*layout)
+        eng.set_tma(tma)
+
+    # 1. plan x layout x staging, built-in tiles: the fastest step
     best = None
     for ex, ey, ez in itertools.product(opts[0], opts[1], opts[2]):
-        if ex:
-            eng.set_plan(0, ex)
-        if ey:
-            eng.set_plan(1, ey)
-        if ez:
-            eng.set_plan(2, ez)
-        times, _ = measure(eng, x, s, y)
-        tiles = {}
-        pipes = {}
-        clusters = {}
-        total = 0.0
-        pts = eng.tuning()["points"]
-        for kind, t0 in times.items():
-            bt, bl, bp = t0, 0, 0
-            bc = (0, 0)
-            # launch forms exist for the compile-time power-of-two kernels
-            # (the pipelined one in FP32 only)
-            axis = {"c2c_x": 0, "c2c_y": 1, "c2c_z": 2}.get(kind, 0 if fmt == 1 else 2)
-            n = (nx, ny, nz)[axis]
-            if kind == "xy_fused" or not pts[axis] or n & (n - 1):
-                forms = [(0, (0, 0))]
-            else:
-                forms = [f for f in LAUNCHES if prec == 4 or f[0] == 0]
-            for depth, clus in forms:
-                eng.set_pipeline(kind, depth)
-                eng.set_cluster(kind, *clus)
-                for L in [0] + TILES:
-                    try:
-                        eng.set_tile(kind, L)
-                    except gbfft.GbfftError:
-                        continue
-                    t = measure(eng, x, s, y, steps=4, warm=1)[0].get(kind, t0)
-                    # a choice other than the built-in one must win by 1 %
-                    if t < bt and t < t0 * MARGIN:
-                        bt, bl, bp, bc = t, L, depth, clus
-                    eng.set_tile(kind, 0)
-            eng.set_pipeline(kind, 0)
-            eng.set_cluster(kind, 0, 0)
-            tiles[kind] = bl
-            pipes[kind] = bp
-            clusters[kind] = bc
-            mult = 2 if kind.startswith("c2c") else 1
-            total += mult * bt
-        log("  plan e_x=%s e_y=%s e_z=%s: est %.4f ms tiles %s pipes %s clusters %s" % (
-            ex, ey, ez, total, tiles, pipes, clusters))
-        if best is None or total < best[0]:
-            best = (total, ex, ey, ez, tiles, pipes, clusters)
-    total, ex, ey, ez, tiles, pipes, clusters = best
-    if ex:
-        eng.set_plan(0, ex)
-    if ey:
-        eng.set_plan(1, ey)
-    if ez:
-        eng.set_plan(2, ez)
+        for layout in LAYOUTS:
+            for tma in (True, False):
+                apply(ex, ey, ez, layout, tma)
+                _, st = measure(eng, x, s, y)
+                log("  e_x=%s e_y=%s e_z=%s pad=%d flat=%d tma=%d: %.4f ms" % (
+                    ex, ey, ez, layout[0], layout[1], tma, st))
+                # the built-in layout and staging unless another wins by 1 %
+                builtin = layout == LAYOUTS[0] and tma
+                key = st if builtin else st / MARGIN
+                if best is None or key < best[0]:
+                    best = (key, ex, ey, ez, layout, tma)
+    _, ex, ey, ez, layout, tma = best
+    apply(ex, ey, ez, layout, tma)
+
+    # 2. tile shape and launch form of every pass kind
+    times, _ = measure(eng, x, s, y)
+    pts = eng.tuning()["points"]
+    tiles, clusters = {}, {}
+    for kind, t0 in times.items():
+        bt, bl, bc = t0, 0, (0, 0)
+        axis = {"c2c_x": 0, "c2c_y": 1, "c2c_z": 2}.get(kind, 0 if fmt == 1 else 2)
+        n = (nx, ny, nz)[axis]
+        # cluster launches exist for the compile-time power-of-two kernels
+        forms = [(0, 0)] if (kind == "xy_fused" or not pts[axis] or n & (n - 1)) else LAUNCHES
+        for clus in forms:
+            eng.set_cluster(kind, *clus)
+            for L in [0] + TILES:
+                try:
+                    eng.set_tile(kind, L)
+                except gbfft.GbfftError:
+                    continue
+                t = measure(eng, x, s, y, steps=4, warm=1)[0].get(kind, t0)
+                # a choice other than the built-in one must win by 1 %
+                if t < bt and t < t0 * MARGIN:
+                    bt, bl, bc = t, L, clus
+                eng.set_tile(kind, 0)
+        eng.set_cluster(kind, 0, 0)
+        tiles[kind] = bl
+        clusters[kind] = bc
     for kind, L in tiles.items():
         if L:
             eng.set_tile(kind, L)
-    for kind, d in pipes.items():
-        if d:
-            eng.set_pipeline(kind, d)
     for kind, c in clusters.items():
         if c[0]:
             eng.set_cluster(kind, *c)
-    # row layout, the built-in one (unpadded rows, flat z passes over
-    # misaligned planes) unless another wins the step by 1 %
-    layout = (0, True)
-    _, step_base = measure(eng, x, s, y)
-    for lay in ((1, True), (2, True), (0, False), (1, False)):
-        eng.set_layout(*lay)
-        _, st = measure(eng, x, s, y)
-        log("  layout pad=%d flat=%d: %.4f ms (built-in %.4f)" % (lay[0], lay[1], st, step_base))
-        if st < step_base * MARGIN:
-            layout, step_base = lay, st
-    eng.set_layout(*layout)
+    log("  tiles %s clusters %s" % (tiles, clusters))
+
+    # 3. pass fusion
     _, step_plain = measure(eng, x, s, y)
     fuse = 0
     eng.set_fusion(True)
@@ -177,6 +163,8 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
         fields.append("pad=%d" % layout[0])
     if not layout[1]:
         fields.append("flat=0")
+    if not tma:
+        fields.append("tma=0")
     if ex:
         fields.append("e_x=%d" % ex)
     if ey:
@@ -186,9 +174,6 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     for kind, L in sorted(tiles.items()):
         if L:
             fields.append("%s=%d" % (kind, L))
-    for kind, d in sorted(pipes.items()):
-        if d:
-            fields.append("pipe_%s=%d" % (kind, d))
     for kind, c in sorted(clusters.items()):
         if c[0]:
             fields.append("cl_%s=%d" % (kind, c[0]))
@@ -207,8 +192,8 @@ def main():
     gbfft.set_tune_cache("")  # measure from the built-in choices
     lines = ["# GB300 tuning cache written by tune.py: prec format nx ny nz key=value ...",
              "# keys: fuse, e_x/e_y/e_z (points per thread of the axis plans), lines per CTA per pass,",
-             "# pipe_<pass> (tile buffers of the pipelined kernel), cl_<pass> / cls_<pass> (cluster",
-             "# launch: CTAs a cluster / start barrier), pad / flat (row layout)"]
+             "# cl_<pass> / cls_<pass> (cluster launch: CTAs a cluster / start barrier), pad / flat",
+             "# (row layout), tma (strided passes staged by bulk tensor copies; default 1)"]
     for shp in shapes:
         print("shape", shp, flush=True)
         line, ms = tune_shape(*shp)

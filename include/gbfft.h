@@ -177,15 +177,6 @@ int gbfft_engine_set_profiling(gbfft_engine_t engine, int enable);
  * the kernel's thread or shared-memory limit. */
 int gbfft_engine_set_tile(gbfft_engine_t engine, int kind, int lines_per_cta);
 
-/* Pipelining of one pass kind (GBFFT_PASS_*), FP32 axes of 256, 512 or
- * 1024 points with a power-of-two plan: depth 2 or 3 runs the pass as a
- * persistent kernel whose CTAs stream tiles through that many shared-memory
- * buffers with asynchronous copies (the loads of the next tiles in flight
- * while one is transformed); 0 (default) runs one CTA per tile.  Other
- * passes ignore it.  gbfft_engine_get_pipeline fills GBFFT_PASS_KINDS ints. */
-int gbfft_engine_set_pipeline(gbfft_engine_t engine, int kind, int depth);
-int gbfft_engine_get_pipeline(gbfft_engine_t engine, int* depth);
-
 /* Cluster launch of one pass kind (GBFFT_PASS_*) on its power-of-two
  * one-shot kernel: ctas 2, 4 or 8 launches neighbouring CTAs (neighbouring
  * lines) as thread-block clusters, which the GPU co-schedules, and sync = 1
@@ -235,6 +226,17 @@ typedef struct {
 int gbfft_plan_describe(int format, int nx, int ny, int nz, int inplace, const int* skip, int prec, int pad,
                         int flat, int which, gbfft_pass_desc_t* out, int max_passes, int* n_passes);
 
+/* Bulk-tensor-copy staging of the strided passes: 1 (default) runs every
+ * strided FP32 c2c pass of 256, 512 or 1024 points whose source rows and
+ * planes lie multiples of 16 bytes apart (the padded work area, rows of an
+ * even number of values) as one persistent kernel per pass, one CTA per SM,
+ * whose tiles arrive in shared memory by cp.async.bulk.tensor copies two
+ * tiles ahead of the one being transformed; 0 runs the one-shot kernel.
+ * A pass whose bounded wait for its copies gives up sets the status that
+ * gbfft_engine_status reports.  Tuning-cache key tma=0/1. */
+int gbfft_engine_set_tma(gbfft_engine_t engine, int enable);
+int gbfft_engine_get_tma(gbfft_engine_t engine, int* enable);
+
 /* Pass fusion: 1 (default) lets the engine run the x and y passes of each
  * z-plane in one kernel where a fused kernel exists for the lengths; 0 runs
  * one kernel per axis. */
@@ -244,11 +246,11 @@ int gbfft_engine_set_fusion(gbfft_engine_t engine, int enable);
  * Engines apply a tuning cache at creation: a text file (default
  * tune_cache.txt in the package directory, or $GBFFT_TUNE_CACHE; "" = none)
  * with lines "prec format nx ny nz key=value ...": per pass kind the lines
- * per CTA (r2c c2r c2c_x c2c_y c2c_z xy_fused), the pipeline depth per pass
- * kind (pipe_r2c, pipe_c2r, pipe_c2c_x, ...), the cluster launch per pass
- * kind (cl_<pass> = CTAs a cluster, cls_<pass> = 1 for the start barrier),
- * fuse=0/1, and e_x / e_y / e_z,
- * the points per thread of the x / y / z plan (as gbfft_engine_set_plan).  The tuner
+ * per CTA (r2c c2r c2c_x c2c_y c2c_z xy_fused) and the cluster launch
+ * (cl_<pass> = CTAs a cluster, cls_<pass> = 1 for the start barrier),
+ * fuse=0/1, pad= / flat= (gbfft_engine_set_layout), tma=0/1
+ * (gbfft_engine_set_tma), and e_x / e_y / e_z, the points per thread of the
+ * x / y / z plan (as gbfft_engine_set_plan).  The tuner
  * (2decomp-fft_gb300/tune.py) measures the choices and writes the file. */
 int gbfft_tune_cache_path(const char* path); /* NULL = default, "" = none */
 /* Re-plan axis 0, 1 or 2: 512 or 1024 points with 16 or 32 points per
@@ -310,6 +312,9 @@ int gbfft_selftest_bounded_wait(int counter_value, int need, long long poll_limi
  * enqueued since load), for benchmarks that report launches. */
 int gbfft_version(int* major, int* minor);
 long long gbfft_launch_count(void);
+/* Of those, the strided passes run by the bulk-tensor-copy kernel
+ * (gbfft_engine_set_tma). */
+long long gbfft_tma_pass_count(void);
 
 /* ---- real-to-real transforms (DCT / DST) ----------------------------------
  * decomp_2d_dtt_3d_r2r and the opt_DTT configuration of decomp_2d_fft_init

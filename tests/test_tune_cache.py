@@ -17,18 +17,16 @@ def allowed(key, v):
         return v in (0, 1)
     if key == "pad":
         return v in (0, 1, 2)
-    if key == "flat":
+    if key in ("flat", "tma"):
         return v in (0, 1)
     if key in ("e_x", "e_y", "e_z"):
         return v in (2, 9, 16, 20, 24, 30, 32)
-    m = re.fullmatch(r"(pipe_|cl_|cls_)?(\w+)", key)
+    m = re.fullmatch(r"(cl_|cls_)?(\w+)", key)
     if not m or m.group(2) not in PASSES:
         return False
     prefix = m.group(1) or ""
     if prefix == "":
         return v in (1, 2, 4, 8, 16, 32)  # lines per CTA
-    if prefix == "pipe_":
-        return v in (2, 3)
     if prefix == "cl_":
         return v in (2, 4, 8)
     return v in (0, 1)  # cls_
