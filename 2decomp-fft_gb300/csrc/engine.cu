@@ -586,10 +586,11 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C, e->tile_L[GBFFT_PASS_C2C_X + axis],
             e->form == GBFFT_FORM_SPLIT, e->csize[GBFFT_PASS_C2C_X + axis],
             e->csync[GBFFT_PASS_C2C_X + axis]);
-  // strided power-of-two FP32 passes over rows a tensor map can describe:
-  // the persistent kernel whose tiles arrive by bulk tensor copies (its plan
-  // shares the axis's stage-major twiddle table)
-  if (e->tma && e->d_status && a.fast == 1 && tma_pass_supported(e->prec, K_C2C, P.contiguous, a)) {
+  // 1024-point FP32 y passes over rows a tensor map can describe: the
+  // persistent kernel whose tiles arrive by bulk tensor copies (its plan
+  // shares the axis's stage-major twiddle table).  Shorter lines and z
+  // passes stay on the one-shot kernel, which is as fast or faster there.
+  if (e->tma && e->d_status && axis == 1 && a.fast == 1 && tma_pass_supported(e->prec, K_C2C, P.contiguous, a)) {
     a.tma = 1;
     a.status = e->d_status;
     a.csize = 0;

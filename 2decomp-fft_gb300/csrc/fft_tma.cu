@@ -1,4 +1,4 @@
-// TMA-staged strided c2c passes (FP32; lines of 256, 512 or 1024 points).
+// TMA-staged strided c2c passes (FP32 y passes; lines of 1024 points).
 //
 // The one-shot strided kernel (fft_fast.cuh) holds its whole tile in
 // registers from its global loads to its first exchange, so an SM has at
@@ -27,6 +27,14 @@
 //    thread that gives up records GBFFT_ERR_TIMEOUT in the engine's status
 //    word, and the producer waits (bounded) for its copies still in flight
 //    and for its stores before the CTA ends.
+//
+// Where it pays (GB300, FP32): y passes of 1024 points, whose one-shot tiles
+// are 64-byte row segments held in 128 registers a thread -- 0.645 ms
+// against 0.82 for a 1024 x 1024 x 512 grid's y pass (rows padded to 64
+// bytes), 6.7 TB/s.  The same kernel on 512- and 256-point lines and on z
+// passes (every row of a tile in another plane) measured slower than the
+// one-shot kernel, which already streams those at 6.3-6.8 TB/s, so the
+// engine uses it for 1024-point y passes only.
 //
 // The tensor maps describe the source and destination arrays as
 // (u, n, v) = (line, point, plane) -- y passes -- or as (u, v, n) when v has
@@ -428,8 +436,8 @@ bool side_ok(const void* base, long long s_n, long long s_l, const PassArgs& a) 
 
 bool tma_pass_supported(int prec_bytes, int kind, bool contiguous, const PassArgs& a) {
   if (prec_bytes != 4 || kind != K_C2C || contiguous || a.row_w != 0) return false;
-  if (a.n != 256 && a.n != 512 && a.n != 1024) return false;
-  if (a.tpl != a.n / 16 && !(a.n >= 512 && a.tpl == a.n / 32)) return false;
+  if (a.n != 1024) return false;
+  if (a.tpl != a.n / 16 && a.tpl != a.n / 32) return false;
   if (a.nlines <= 0 || a.nv <= 0 || a.nlines > (1ll << 31) || a.nv > (1ll << 31)) return false;
   if (!a.src || !a.dst || !a.tw) return false;
   if ((a.s_src_l < a.s_src_n) != (a.s_dst_l < a.s_dst_n)) return false;
@@ -440,12 +448,8 @@ bool tma_pass_supported(int prec_bytes, int kind, bool contiguous, const PassArg
 long long tma_launch_counter() { return tma::g_tma_launches.load(); }
 
 cudaError_t launch_tma_pass(const PassArgs& a, cudaStream_t stream) {
-  switch (a.n) {
-    case 256: return tma::launch_n<256>(a, stream);
-    case 512: return tma::launch_n<512>(a, stream);
-    case 1024: return tma::launch_n<1024>(a, stream);
-    default: return cudaErrorNotSupported;
-  }
+  if (a.n != 1024) return cudaErrorNotSupported;
+  return tma::launch_n<1024>(a, stream);
 }
 
 }  // namespace gbfft

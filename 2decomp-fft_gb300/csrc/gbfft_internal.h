@@ -258,11 +258,10 @@ __host__ __device__ constexpr bool dtt_fast_length(int M) { return M >= 32 && M 
 __host__ __device__ constexpr bool dtt_mixed_length(int M) { return M == 126 || M == 510; }
 cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream);
 
-// TMA-staged strided c2c passes (fft_tma.cu): FP32 lines of 256, 512 or
-// 1024 points whose source rows and planes lie multiples of 16 bytes apart
-// and start 16-byte aligned, on the axis's own compile-time plan (a.tpl =
-// n / 16, or n / 32 for 512 and 1024 points; the stage-major twiddle table
-// is the axis's).
+// TMA-staged strided c2c passes (fft_tma.cu): FP32 lines of 1024 points
+// whose source and destination rows and planes lie multiples of 16 bytes
+// apart and start 16-byte aligned, on the axis's own compile-time plan
+// (a.tpl = n / 16 or n / 32; the stage-major twiddle table is the axis's).
 bool tma_pass_supported(int prec_bytes, int kind, bool contiguous, const PassArgs& a);
 cudaError_t launch_tma_pass(const PassArgs& a, cudaStream_t stream);
 long long tma_launch_counter();

@@ -226,12 +226,12 @@ typedef struct {
 int gbfft_plan_describe(int format, int nx, int ny, int nz, int inplace, const int* skip, int prec, int pad,
                         int flat, int which, gbfft_pass_desc_t* out, int max_passes, int* n_passes);
 
-/* Bulk-tensor-copy staging of the strided passes: 1 (default) runs every
- * strided FP32 c2c pass of 256, 512 or 1024 points whose source rows and
- * planes lie multiples of 16 bytes apart (the padded work area, rows of an
- * even number of values) as one persistent kernel per pass, one CTA per SM,
- * whose tiles arrive in shared memory by cp.async.bulk.tensor copies two
- * tiles ahead of the one being transformed; 0 runs the one-shot kernel.
+/* Bulk-tensor-copy staging of the y passes: 1 (default) runs every FP32 c2c
+ * y pass of 1024 points whose rows and planes lie multiples of 16 bytes
+ * apart (the padded work area, rows of an even number of values) as one
+ * persistent kernel per pass, one CTA per SM, whose tiles arrive in shared
+ * memory by cp.async.bulk.tensor copies two tiles ahead of the one being
+ * transformed and leave it the same way; 0 runs the one-shot kernel.
  * A pass whose bounded wait for its copies gives up sets the status that
  * gbfft_engine_status reports.  Tuning-cache key tma=0/1. */
 int gbfft_engine_set_tma(gbfft_engine_t engine, int enable);

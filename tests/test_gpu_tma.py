@@ -1,14 +1,15 @@
-"""GPU: strided passes staged by bulk tensor copies (gbfft_engine_set_tma)
+"""GPU: 1024-point y passes staged by bulk tensor copies (gbfft_engine_set_tma)
 against the oracle, and against the one-shot kernel they stand in for (same
 plan, same twiddle table, same butterflies; the two kernels agree to
 rounding -- rel-L2 <= 1e-6 -- since the compiler may fuse the complex
 multiply-adds into FMAs differently in each).
 
-Covered: y and z passes of 256, 512 and 1024 points; ragged last tiles (line
-counts that are not a multiple of the tile's lines, and fewer lines than one
-tile); one plane; c2c in both directions and formats; r2c / c2r in the padded
-work area (pad=1) and in Z-format rows; the 1024 x 1024 x 512 FP32 grid with
-the padded layout against the exact spectrum of the reference's test field.
+Covered: both plans of 1024 points (16 and 32 points a thread); ragged last
+tiles (line counts that are not a multiple of the tile's lines, and fewer
+lines than one tile); one plane; c2c in both directions and formats; r2c /
+c2r in the padded work area (pad=1, 2) and in Z-format rows; the
+1024 x 1024 x 512 FP32 grid with the padded layout against the exact spectrum
+of the reference's test field.
 Tolerance against the FP64 oracle: relative L2 <= 2e-6 (single precision).
 """
 import numpy as np
@@ -39,13 +40,14 @@ def _engine(fmt, shape, tma, pad=None):
 
 # every shape has at least one eligible strided pass: y passes over rows of
 # an even number of values, z passes over rows of a multiple of 16 values
-C2C_SHAPES = [(64, 1024, 6), (30, 1024, 3), (6, 1024, 2), (40, 512, 10), (2, 512, 4), (256, 256, 12),
-              (16, 24, 256), (32, 6, 512), (16, 5, 1024), (10, 256, 1)]
+# (shape, points a thread of the y plan): rows of an even number of values
+C2C_SHAPES = [((64, 1024, 6), 32), ((64, 1024, 6), 16), ((30, 1024, 3), 16), ((6, 1024, 2), 32),
+              ((2, 1024, 4), 16), ((10, 1024, 1), 16), ((1024, 1024, 2), 16)]
 
 
 @pytest.mark.parametrize("fmt", [O.PHYSICAL_IN_X, O.PHYSICAL_IN_Z])
-@pytest.mark.parametrize("shape", C2C_SHAPES)
-def test_c2c_tma_against_oracle_and_one_shot(fmt, shape):
+@pytest.mark.parametrize("shape,ey", C2C_SHAPES)
+def test_c2c_tma_against_oracle_and_one_shot(fmt, shape, ey):
     import gbfft
     nx, ny, nz = shape
     rng = np.random.default_rng(nx * 7 + ny * 3 + nz + fmt)
@@ -56,16 +58,14 @@ def test_c2c_tma_against_oracle_and_one_shot(fmt, shape):
         outs = []
         for tma in (True, False):
             e = _engine(fmt, shape, tma)
+            e.set_plan(1, ey)
             y = torch.empty_like(x)
             c0 = gbfft.tma_pass_count()
             e.c2c(x, y, isign)
             torch.cuda.synchronize()
             e.status()
             ran = gbfft.tma_pass_count() - c0
-            if tma:
-                assert ran >= 1  # every shape here has an eligible strided pass
-            else:
-                assert ran == 0
+            assert ran == (1 if tma else 0)  # the y pass
             outs.append(y.cpu().numpy())
             e.close()
         assert rel(outs[0], ref) <= TOL
@@ -75,10 +75,10 @@ def test_c2c_tma_against_oracle_and_one_shot(fmt, shape):
 # (format, shape, pad, TMA passes of one r2c + c2r): X-format y passes run
 # it in the padded work area (pad=1 both directions, pad=2 c2r only),
 # Z-format y passes over rows of an even number of values
-REAL_CASES = [(O.PHYSICAL_IN_X, (1024, 256, 6), 1, 2), (O.PHYSICAL_IN_X, (62, 512, 5), 1, 2),
+REAL_CASES = [(O.PHYSICAL_IN_X, (1024, 1024, 6), 1, 2), (O.PHYSICAL_IN_X, (62, 1024, 5), 1, 2),
               (O.PHYSICAL_IN_X, (1022, 1024, 2), 1, 2), (O.PHYSICAL_IN_X, (512, 1024, 3), 2, 1),
-              (O.PHYSICAL_IN_Z, (64, 512, 10), 0, 2), (O.PHYSICAL_IN_Z, (34, 1024, 7), 0, 2),
-              (O.PHYSICAL_IN_Z, (256, 256, 9), 1, 2)]
+              (O.PHYSICAL_IN_X, (512, 1024, 3), 0, 0), (O.PHYSICAL_IN_Z, (64, 1024, 10), 0, 2),
+              (O.PHYSICAL_IN_Z, (34, 1024, 7), 0, 2), (O.PHYSICAL_IN_Z, (256, 1024, 9), 1, 2)]
 
 
 @pytest.mark.parametrize("fmt,shape,pad,expect", REAL_CASES)
@@ -93,6 +93,8 @@ def test_r2c_c2r_tma_against_oracle_and_one_shot(fmt, shape, pad, expect):
     got = {}
     for tma in (True, False):
         e = _engine(fmt, shape, tma, pad)
+        e.set_plan(1, 16)
+        e.set_layout(pad=pad, flat=True)
         xd = torch.from_numpy(x).cuda()
         spec = e.empty_spectral()
         c0 = gbfft.tma_pass_count()
@@ -120,6 +122,8 @@ def test_large_grid_padded_layout_against_exact_spectrum():
     import gbfft
     nx, ny, nz = 1024, 1024, 512
     e = _engine(O.PHYSICAL_IN_X, (nx, ny, nz), True, pad=1)
+    e.set_plan(1, 16)
+    e.set_layout(pad=1, flat=True)
     x = torch.from_numpy(G.field(nx, ny, nz, np.float32)).cuda()
     spec = e.empty_spectral()
     c0 = gbfft.tma_pass_count()
