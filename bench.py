@@ -180,6 +180,75 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+# host side of the end-to-end leg
+# ---------------------------------------------------------------------------
+def gpu_local_cpus(dev_index):
+    """CPUs of the GPU's NUMA node (sysfs local_cpulist of its PCI device),
+    restricted to this process's affinity; empty when unknown."""
+    import torch
+    try:
+        p = torch.cuda.get_device_properties(dev_index)
+        bus = "%04x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+        text = open("/sys/bus/pci/devices/%s/local_cpulist" % bus).read().strip()
+    except Exception:
+        return set()
+    cpus = set()
+    for part in text.split(","):
+        part = part.strip()
+        if "-" in part:
+            a, b = part.split("-")
+            cpus |= set(range(int(a), int(b) + 1))
+        elif part:
+            cpus.add(int(part))
+    return cpus & set(os.sched_getaffinity(0))
+
+
+def bind_near_gpu(dev_index):
+    """Run this process on the GPU's NUMA node, so that pinned host buffers
+    allocated afterwards sit next to the GPU.  Returns the CPU list used."""
+    cpus = gpu_local_cpus(dev_index)
+    if cpus and cpus != set(os.sched_getaffinity(0)):
+        try:
+            os.sched_setaffinity(0, cpus)
+        except Exception:
+            pass
+    return sorted(os.sched_getaffinity(0))
+
+
+def link_gbs(host, dev, stream, reps=3):
+    """Host-link bandwidth seen by this process: host->device, device->host
+    and both at once (each direction), GB/s, copies of `host` (pinned) to
+    and from `dev` timed with CUDA events."""
+    import torch
+    nb = host.numel() * host.element_size()
+    other = torch.cuda.Stream(dev.device)
+    dev2 = torch.empty_like(dev)
+    host2 = torch.empty_like(host, pin_memory=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    for name, fn in (("h2d", lambda: dev.copy_(host, non_blocking=True)),
+                     ("d2h", lambda: host.copy_(dev, non_blocking=True))):
+        with torch.cuda.stream(stream):
+            fn()
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = round(reps * nb / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            dev.copy_(host, non_blocking=True)
+        with torch.cuda.stream(other):
+            host2.copy_(dev2, non_blocking=True)
+    torch.cuda.synchronize()
+    out["both_each"] = round(reps * nb / (time.perf_counter() - t) / 1e9, 1)
+    return out
+
+
+# ---------------------------------------------------------------------------
 # inputs
 # ---------------------------------------------------------------------------
 def make_input(nx, ny, nz, kind, dtype, device):
@@ -332,6 +401,7 @@ def run_gb300(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    cpus = bind_near_gpu(local)
     nx, ny, nz, fmt, prec, kind = WORKLOADS[args.workload]
     rdt = torch.float32 if prec == 4 else torch.float64
     gbfft.lib()
@@ -427,6 +497,7 @@ def run_gb300(args):
     yh = torch.empty_like(xh, pin_memory=True)
     xd = torch.empty_like(x)
     e2e_steps = max(3, min(args.steps, 20))
+    link = link_gbs(xh, xd, stream)
 
     def e2e_step():
         xd.copy_(xh, non_blocking=True)
@@ -500,6 +571,11 @@ def run_gb300(args):
            "d2h_bytes_per_step": y.numel() * y.element_size(),
            "form": "copies of step i+1 / i-1 overlap the transforms of step i (double-buffered)",
            "results_identical_across_steps": same,
+           "host_link_gbs": link,
+           "host_cpus": "%d CPUs on the GPU's NUMA node (%s)" % (len(cpus), "bound" if gpu_local_cpus(local) else
+                                                                 "node unknown: not bound"),
+           "link_bound_ms": round(max(x.numel() * x.element_size() / (link["both_each"] * 1e9),
+                                      y.numel() * y.element_size() / (link["both_each"] * 1e9)) * 1e3, 3),
            "serial": {"value": round(total_pts / (serial_ms * 1e-3) / 1e9, 3), "ms_per_step": round(serial_ms, 3),
                       "form": "copy in, r2c, c2r, copy out on one stream"}}
 
