@@ -408,7 +408,8 @@ size_t dtt_smem_bytes(int prec_bytes, int M, int L) {
   return (2 * (e + (e >> 4) + 1) + (size_t)M) * (size_t)(2 * prec_bytes);  // two line buffers, twiddles
 }
 
-cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream) {
+namespace {
+cudaError_t launch_dtt_one(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream) {
   if (a.n < 1 || a.M < 2 || a.L < 1 || a.tpl < 1) return cudaErrorInvalidValue;
   if (a.twf && dtt_mixed_length(a.M)) {
     // FP32 only: the engine keeps FP64 on the runtime plan
@@ -423,6 +424,23 @@ cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, c
   if (a.L * a.tpl > kMaxThreads) return cudaErrorInvalidValue;
   if (prec_bytes == 4) return contiguous ? launch_t<float, true>(a, stream) : launch_t<float, false>(a, stream);
   return contiguous ? launch_t<double, true>(a, stream) : launch_t<double, false>(a, stream);
+}
+}  // namespace
+
+// Strided passes with more planes than a grid's y extent allows run as
+// several launches of at most kMaxGridY planes, the arrays offset by the
+// planes already done (a line (u, v) starts at u + v * sl).
+cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, cudaStream_t stream) {
+  if (contiguous || a.nv <= kMaxGridY) return launch_dtt_one(prec_bytes, contiguous, a, stream);
+  for (long long v0 = 0; v0 < a.nv; v0 += kMaxGridY) {
+    DttArgs b = a;
+    b.nv = (int)(a.nv - v0 < kMaxGridY ? a.nv - v0 : kMaxGridY);
+    b.src = static_cast<const char*>(a.src) + v0 * a.sl * prec_bytes;
+    b.dst = static_cast<char*>(a.dst) + v0 * a.sl * prec_bytes;
+    cudaError_t err = launch_dtt_one(prec_bytes, contiguous, b, stream);
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace gbfft

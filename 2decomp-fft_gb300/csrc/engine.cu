@@ -54,13 +54,16 @@ struct AxisPlan {
   int radix[kMaxStages] = {0};
   int tpl = 1;        // threads per line
   int fast_e = 16;    // points per thread of the power-of-two kernel
+  bool big = false;   // lines do not fit one shared-memory tile: the
+                      // multi-kernel long-axis path (fft_long.cu)
   void* d_tw = nullptr;   // exp(-2 pi i m / n), m = 0..n-1
   void* d_twf = nullptr;  // stage-major table of the power-of-two kernel
 };
 
 // Split n into radix stages: 16s, then one 8/4/2 for the rest of the powers
-// of two, then 3s, 5s, 7s, then any other prime as a generic stage.  Largest
-// radices first.
+// of two, then 7s, 5s, 3s, then any other prime as a generic stage.  Largest
+// radices first.  Any length factorises; whether its lines fit one tile is
+// decided by the caller.
 bool factorize(int n, AxisPlan& p, std::string& why) {
   std::vector<int> r;
   int m = n;
@@ -100,11 +103,6 @@ bool factorize(int n, AxisPlan& p, std::string& why) {
   int tpl = (n + 7) / 8;
   if (tpl > kMaxThreads) tpl = kMaxThreads;
   if (tpl < 1) tpl = 1;
-  if (n > kMaxN) {
-    why = "axis length " + std::to_string(n) + " exceeds the single-tile limit of " +
-          std::to_string(kMaxN);
-    return false;
-  }
   p.tpl = tpl;
   return true;
 }
@@ -317,6 +315,9 @@ struct gbfft_engine_s {
   // allow it run the persistent kernel fed by bulk tensor copies
   bool tma = true;
   int* d_status = nullptr;  // set to 1 by a bounded wait that gave up
+  // two buffers of the grid's size for axes on the long-axis path
+  void* long_scratch = nullptr;
+  size_t long_scratch_bytes = 0;
 };
 
 namespace {
@@ -345,6 +346,8 @@ void release(gbfft_engine_t e) {
   e->d_sync = nullptr;
   if (e->d_status) cudaFree(e->d_status);
   e->d_status = nullptr;
+  if (e->long_scratch) cudaFree(e->long_scratch);
+  e->long_scratch = nullptr;
 }
 
 size_t cbytes(const gbfft_engine_s* e) { return 2 * (size_t)e->prec; }
@@ -535,6 +538,7 @@ struct Pass {
   int prof_kind;   // GBFFT_PASS_*
   double bytes;    // algorithmic bytes: one read + one write of the array
   bool fused = false;  // x and y passes of each z-plane in one kernel
+  bool big = false;    // long-axis path (one kernel per radix stage)
   FusedArgs f;
   int fused_kindx = 0;
   bool fused_xfirst = true;
@@ -575,7 +579,7 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
     a.s_dst_l = pout;
     a.nlines = n1;
     a.nv = n2;
-    if (e->flat && pout == n1 && !rows_aligned(n1, cbytes(e))) {
+    if (e->flat && pout == n1 && !rows_aligned(n1, cbytes(e)) && !e->ax[axis].big) {
       a.nlines = n1 * n2;
       a.nv = 1;
       a.row_w = n1;
@@ -596,6 +600,7 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
     a.csize = 0;
     a.csync = 0;
   }
+  P.big = e->ax[axis].big;
   P.prof_kind = GBFFT_PASS_C2C_X + axis;
   P.bytes = 2.0 * (double)n1 * n2 * n3 * (double)cbytes(e);
   return P;
@@ -630,7 +635,8 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst, lo
     a.real_lines = nx;
     a.nv = ny;
     // the output rows: complex (pitch cp) for r2c, real (nx) for c2r
-    flat = e->flat && (kind == K_C2R ? !rows_aligned(nx, (size_t)e->prec) : (cp == nx && !rows_aligned(nx, cbytes(e))));
+    flat = e->flat && !e->ax[2].big &&
+           (kind == K_C2R ? !rows_aligned(nx, (size_t)e->prec) : (cp == nx && !rows_aligned(nx, cbytes(e))));
     if (flat) {
       a.real_lines = nx * ny;
       a.nv = 1;
@@ -669,6 +675,7 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst, lo
             e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R], e->form == GBFFT_FORM_SPLIT,
             e->csize[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R],
             e->csync[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R]);
+  P.big = e->ax[axis].big;
   P.prof_kind = kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R;
   P.bytes = (double)nx * ny * nz * e->prec +
             (double)e->sp[0] * e->sp[1] * e->sp[2] * (double)cbytes(e);
@@ -734,8 +741,6 @@ void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
 
 int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st) {
   for (const Pass& p : ps) {
-    if (!p.contiguous && p.a.nv > 65535 && !p.a.tma)
-      return fail(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
     ProfRec rec{p.prof_kind, nullptr, nullptr, p.bytes};
     if (e->profiling) {
       if (cudaEventCreate(&rec.start) != cudaSuccess || cudaEventCreate(&rec.stop) != cudaSuccess)
@@ -743,6 +748,8 @@ int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st) 
       cudaEventRecord(rec.start, st);
     }
     cudaError_t err = p.fused ? launch_fused(e->prec, p.fused_kindx, p.fused_xfirst, p.f, st)
+                      : p.big ? launch_long_pass(e->prec, p.kind, p.contiguous, p.a, e->long_scratch,
+                                                 e->long_scratch_bytes, st)
                               : launch_axis_pass(e->prec, p.kind, p.contiguous, p.a, st);
     if (e->profiling) {
       cudaEventRecord(rec.stop, st);
@@ -819,9 +826,8 @@ int engine_init_host(gbfft_engine_s* e, int format, int nx, int ny, int nz, int 
   for (int d = 0; d < 3; ++d) {
     std::string why;
     if (!factorize(lens[d], e->ax[d], why)) return fail(GBFFT_ERR_UNSUPPORTED, why);
-    if (pass_smem_bytes(prec, lens[d], 1) > 200 * 1024)
-      return fail(GBFFT_ERR_UNSUPPORTED, "axis length " + std::to_string(lens[d]) +
-                                             " does not fit one shared-memory tile at this precision");
+    // lines longer than one shared-memory tile take the long-axis path
+    e->ax[d].big = lens[d] > kMaxN || pass_smem_bytes(prec, lens[d], 1) > 200 * 1024;
     e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
     if (gen_length(lens[d])) e->ax[d].fast_e = gen_points(lens[d]);
     if (fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
@@ -1039,6 +1045,19 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
     }
     cudaMemset(e->d_status, 0, 4 * sizeof(int));
   }
+  // scratch of the long-axis path: two copies of the largest pass's lines,
+  // at most the whole grid in complex values (any engine may run c2c)
+  if (e->ax[0].big || e->ax[1].big || e->ax[2].big) {
+    e->long_scratch_bytes = 2 * (size_t)nx * ny * nz * cbytes(e);
+    cudaError_t err = cudaMalloc(&e->long_scratch, e->long_scratch_bytes);
+    if (err != cudaSuccess) {
+      e->long_scratch = nullptr;
+      release(e);
+      delete e;
+      g_err = std::string("cudaMalloc(long-axis scratch): ") + cudaGetErrorString(err);
+      return GBFFT_ERR_ALLOC;
+    }
+  }
   apply_tune(e, tune);
   g_err.clear();
   *engine = e;
@@ -1065,7 +1084,7 @@ int gbfft_engine_get_sizes(gbfft_engine_t e, int ph[3], int sp[3]) {
 
 int gbfft_engine_work_bytes(gbfft_engine_t e, size_t* bytes) {
   if (!valid_engine(e) || !bytes) return fail(GBFFT_ERR_INVALID, "bad argument");
-  *bytes = e->work_bytes;
+  *bytes = e->work_bytes + e->long_scratch_bytes;
   return GBFFT_OK;
 }
 
@@ -1503,7 +1522,7 @@ int setup_dtt_axis(DttAxis& a, int kind, int first, int ndismiss, int naxis, int
   a.M = kind == 1 ? 2 * (a.n - 1) : kind == 5 ? 2 * (a.n + 1) : 2 * a.n;
   std::string why;
   if (!factorize(a.M, a.plan, why)) return fail(GBFFT_ERR_UNSUPPORTED, "r2r extension: " + why);
-  if (dtt_smem_bytes(prec, a.M, 1) > 200 * 1024)
+  if (a.M > kMaxN || dtt_smem_bytes(prec, a.M, 1) > 200 * 1024)
     return fail(GBFFT_ERR_UNSUPPORTED, "r2r extension does not fit one shared-memory tile");
   int rc = upload_table(&a.tw, twiddles(a.M), prec);
   if (rc != GBFFT_OK) return rc;
@@ -1652,7 +1671,6 @@ int gbfft_exec_r2r(gbfft_dtt_t d, void* d_in, void* d_out, int isign, void* stre
       a.nv = (int)ny;
       a.naxis = (int)nz;
     }
-    if (!contiguous && a.nv > 65535) return fail(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
     if (ax.twf && dtt_mixed_length(ax.M)) {
       // compile-time two-stage plan: R1 threads a line, at most 256 a CTA;
       // contiguous about 128, strided up to 16 neighbouring lines

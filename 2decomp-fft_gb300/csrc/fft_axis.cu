@@ -155,8 +155,8 @@ size_t pass_smem_bytes(int prec_bytes, int n, int L) {
   return 2 * (e + (e >> 4) + 1) * (size_t)(2 * prec_bytes);
 }
 
-cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a,
-                             cudaStream_t stream) {
+namespace {
+cudaError_t launch_axis_one(int prec_bytes, int kind, bool contiguous, const PassArgs& a, cudaStream_t stream) {
   if (a.tma) {
     if (!tma_pass_supported(prec_bytes, kind, contiguous, a)) return cudaErrorInvalidValue;
     return launch_tma_pass(a, stream);
@@ -193,6 +193,28 @@ cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous, const Pa
   }
 #undef GB_DISPATCH
   return cudaErrorInvalidValue;
+}
+}  // namespace
+
+// Strided one-shot passes with more planes than a grid's y extent allows
+// run as several launches of at most kMaxGridY planes, each side's array
+// offset by the planes already done (a line (u, v) starts at u + v * s_l, in
+// elements of that side's type).  The persistent bulk-copy pass walks any
+// number of planes itself.
+cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a,
+                             cudaStream_t stream) {
+  if (contiguous || a.tma || a.nv <= kMaxGridY) return launch_axis_one(prec_bytes, kind, contiguous, a, stream);
+  const size_t cs = 2 * (size_t)prec_bytes, rs = (size_t)prec_bytes;
+  const size_t src_e = kind == K_R2C ? rs : cs, dst_e = kind == K_C2R ? rs : cs;
+  for (long long v0 = 0; v0 < a.nv; v0 += kMaxGridY) {
+    PassArgs b = a;
+    b.nv = (int)(a.nv - v0 < kMaxGridY ? a.nv - v0 : kMaxGridY);
+    b.src = static_cast<const char*>(a.src) + v0 * a.s_src_l * src_e;
+    b.dst = static_cast<char*>(a.dst) + v0 * a.s_dst_l * dst_e;
+    cudaError_t err = launch_axis_one(prec_bytes, kind, contiguous, b, stream);
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_copy(const void* src, void* dst, size_t bytes, cudaStream_t stream) {

@@ -15,6 +15,7 @@ constexpr int kMaxStages = 16;    // radix stages of one axis plan
 constexpr int kMaxE = 16;         // complex values a thread holds in one stage
 constexpr int kMaxThreads = 512;  // threads in one CTA of an axis pass
 constexpr int kMaxN = 8192;       // longest axis a single-tile pass supports
+constexpr int kMaxGridY = 65535;  // planes (grid.y) of one strided launch
 
 // What one axis pass does to each line.
 enum Kind : int {
@@ -265,6 +266,14 @@ cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, c
 bool tma_pass_supported(int prec_bytes, int kind, bool contiguous, const PassArgs& a);
 cudaError_t launch_tma_pass(const PassArgs& a, cudaStream_t stream);
 long long tma_launch_counter();
+
+// Axis passes whose lines do not fit one shared-memory tile (fft_long.cu):
+// one kernel per radix stage through `scratch`, which must hold two copies
+// of the pass's lines (long_pass_scratch_bytes).  Lines are per row (row_w
+// = 0); a.nst / a.radix are the axis's stages, a.tw its n-root table.
+size_t long_pass_scratch_bytes(int prec_bytes, bool contiguous, const PassArgs& a);
+cudaError_t launch_long_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a, void* scratch,
+                             size_t scratch_bytes, cudaStream_t stream);
 
 // Enqueue one axis pass.  prec_bytes = 4 (float) or 8 (double).
 cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous,

@@ -251,8 +251,6 @@ extern "C" int gbfft_exec_c2r_noalloc(int format, int nx, int ny, int nz, int pr
       a.nlines = s1;
       a.nv = ny;
     }
-    if (!contiguous && a.nv > 65535)
-      return gbfft::set_error(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
     tile(plan[ax], prec, contiguous, a.nlines, a);
     e = gbfft::launch_axis_pass(prec, gbfft::K_C2C, contiguous, a, st);
     if (e != cudaSuccess) return gbfft::set_error(GBFFT_ERR_CUDA, cudaGetErrorString(e));
@@ -279,8 +277,6 @@ extern "C" int gbfft_exec_c2r_noalloc(int format, int nx, int ny, int nz, int pr
     a.s_src_l = a.s_dst_l = nx;
     a.real_lines = nx;
     a.nv = ny;
-    if (a.nv > 65535)
-      return gbfft::set_error(GBFFT_ERR_UNSUPPORTED, "grid extent along the batch axis exceeds 65535");
   }
   a.nlines = (a.real_lines + 1) / 2;
   a.tw = sb + tw_off[ax];

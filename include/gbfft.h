@@ -82,7 +82,11 @@ int gbfft_engine_destroy(gbfft_engine_t engine);
  * (src/fft_common.f90:204-216, :311-327). */
 int gbfft_engine_get_sizes(gbfft_engine_t engine, int ph[3], int sp[3]);
 
-/* Bytes of device work area the engine holds (0 when none is needed). */
+/* Bytes of device work area the engine holds (0 when none is needed): the
+ * c2r / padded-layout work area, plus, when an axis is longer than one
+ * shared-memory tile (more than 8192 points, or an FP64 line whose two
+ * buffers exceed the tile), two grid-sized complex buffers for that axis's
+ * stage-by-stage passes. */
 int gbfft_engine_work_bytes(gbfft_engine_t engine, size_t* bytes);
 
 /* 3D r2c, forward, unnormalised: fft_3d_r2c (src/fft_common_3d.f90:121-189,
