@@ -48,6 +48,11 @@ SIGNATURES = {
     "gbfft_exec_c2c": (_i, [_vp, _vp, _vp, _i, _vp]),
     "gbfft_transpose": (_i, [_i, _i, _i, _vp, _vp, _i, _i, _i, _vp]),
     "gbfft_malloc": (_i, [ctypes.POINTER(_vp), _sz]),
+    "gbfft_decomp_info": (_i, [_i, _i, _i, _i, _i, _i, _vp]),
+    "gbfft_decomp_distribute": (_i, [_i, _i, _ip, _ip, _ip]),
+    "gbfft_decomp_counts": (_i, [_i] * 7 + [_ip] * 7),
+    "gbfft_transpose_pack": (_i, [_i, _i, _i, _vp, _i, _i, _i, _i, _ip, _ip, _vp, _sz, _vp]),
+    "gbfft_transpose_unpack": (_i, [_i, _i, _i, _vp, _i, _i, _i, _i, _ip, _ip, _sz, _vp, _vp]),
     "gbfft_free": (_i, [_vp]),
     "gbfft_last_error_string": (ctypes.c_char_p, []),
     "gbfft_warning_count": (_i, []),
@@ -562,3 +567,249 @@ def decomp_2d_fft_log():
     buf = ctypes.create_string_buffer(1024)
     check(lib().d2d_fft_log(buf, 1024))
     return buf.value.decode()
+
+
+# ---------------------------------------------------------------------------
+# multi-rank pencil transposes (p_row x p_col ranks)
+# ---------------------------------------------------------------------------
+MAX_PEERS = 1024
+
+
+class PencilInfo(ctypes.Structure):
+    """gbfft_pencil_info_t: a rank's sub-block of each pencil (1-based)."""
+    _fields_ = [(n, ctypes.c_int * 3) for n in ("xst", "xen", "xsz", "yst", "yen", "ysz", "zst", "zen", "zsz")] + \
+               [("coord", ctypes.c_int * 2)]
+
+
+def decomp_distribute(n, nproc):
+    """distribute: 1-based starts, ends and sizes of n points over nproc."""
+    a = [(ctypes.c_int * nproc)() for _ in range(3)]
+    check(lib().gbfft_decomp_distribute(int(n), int(nproc), *a))
+    return tuple(list(x) for x in a)
+
+
+class Decomp:
+    """Decomposition of an (nx, ny, nz) grid over a p_row x p_col rank grid,
+    seen from `rank` (row-major: rank = coord1 * p_col + coord2): the
+    rank's pencil sub-blocks (xst/xen/xsz ... , 1-based, Fortran order) and
+    the exchange counts of each transpose."""
+
+    def __init__(self, nx, ny, nz, p_row, p_col, rank):
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        self.p_row, self.p_col, self.rank = int(p_row), int(p_col), int(rank)
+        info = PencilInfo()
+        check(lib().gbfft_decomp_info(self.nx, self.ny, self.nz, self.p_row, self.p_col, self.rank,
+                                      ctypes.byref(info)))
+        for name, _ in PencilInfo._fields_:
+            setattr(self, name, tuple(getattr(info, name)))
+
+    def shape(self, pencil):
+        """numpy / torch view (n3, n2, n1) of the rank's `pencil` ('x', 'y' or 'z')."""
+        sz = getattr(self, pencil + "sz")
+        return (sz[2], sz[1], sz[0])
+
+    def counts(self, kind):
+        """dict of send_dist, send_cnts, send_disp, recv_dist, recv_cnts,
+        recv_disp (lists, one entry per peer of the exchange)."""
+        arrs = [(ctypes.c_int * MAX_PEERS)() for _ in range(6)]
+        n = ctypes.c_int(0)
+        check(lib().gbfft_decomp_counts(self.nx, self.ny, self.nz, self.p_row, self.p_col, self.rank, int(kind),
+                                        *arrs, ctypes.byref(n)))
+        names = ("send_dist", "send_cnts", "send_disp", "recv_dist", "recv_cnts", "recv_disp")
+        return {k: list(a[: n.value]) for k, a in zip(names, arrs)}
+
+
+def _elem(t):
+    import torch
+    cplx = t.dtype in (torch.complex64, torch.complex128)
+    prec = PREC_DOUBLE if t.dtype in (torch.float64, torch.complex128) else PREC_SINGLE
+    return cplx, prec
+
+
+def transpose_pack(kind, src, send, dist, disp, stream=None):
+    """gbfft_transpose_pack: the pencil `src` (numpy view (n3, n2, n1)) into
+    the 1D buffer `send` (device tensors of the same dtype)."""
+    cplx, prec = _elem(src)
+    n3, n2, n1 = src.shape
+    p = len(dist)
+    check(lib().gbfft_transpose_pack(int(kind), int(cplx), prec, _ptr(src), n1, n2, n3, p,
+                                     (ctypes.c_int * p)(*dist), (ctypes.c_int * p)(*disp), _ptr(send),
+                                     send.numel(), _stream(stream)))
+    return send
+
+
+def transpose_unpack(kind, recv, dst, dist, disp, stream=None):
+    """gbfft_transpose_unpack: the received 1D buffer into the pencil `dst`."""
+    cplx, prec = _elem(dst)
+    n3, n2, n1 = dst.shape
+    p = len(dist)
+    check(lib().gbfft_transpose_unpack(int(kind), int(cplx), prec, _ptr(recv), n1, n2, n3, p,
+                                       (ctypes.c_int * p)(*dist), (ctypes.c_int * p)(*disp), recv.numel(),
+                                       _ptr(dst), _stream(stream)))
+    return dst
+
+
+def pencil_groups(p_row, p_col):
+    """The row and column process groups of this rank for a p_row x p_col
+    grid (torch.distributed must be initialised; every rank creates every
+    group, in the same order): ROW = the p_col ranks of one grid row (y <-> z
+    exchanges), COL = the p_row ranks of one grid column (x <-> y)."""
+    import torch.distributed as dist
+    rank = dist.get_rank()
+    row = col = None
+    for c1 in range(p_row):
+        g = dist.new_group([c1 * p_col + c2 for c2 in range(p_col)])
+        if rank // p_col == c1:
+            row = g
+    for c2 in range(p_col):
+        g = dist.new_group([c1 * p_col + c2 for c1 in range(p_row)])
+        if rank % p_col == c2:
+            col = g
+    return row, col
+
+
+def transpose_dist(kind, src, dst, decomp, groups, pack=None, unpack=None):
+    """One transpose between pencils on a p_row x p_col rank grid:
+    pack (gbfft_transpose_pack), ALLTOALLV of the row (y <-> z) or column
+    (x <-> y) group (torch.distributed all_to_all_single: NCCL between GPUs),
+    unpack (gbfft_transpose_unpack) -- transpose_x_to_y and siblings of
+    src/transpose_x_to_y.f90:96-133 etc.  `src` and `dst` are this rank's
+    pencils, `groups` = pencil_groups(p_row, p_col).  With one peer the
+    exchange is a local copy."""
+    import torch
+    import torch.distributed as dist
+    pack = pack or transpose_pack
+    unpack = unpack or transpose_unpack
+    c = decomp.counts(kind)
+    send = torch.empty(sum(c["send_cnts"]), dtype=src.dtype, device=src.device)
+    recv = torch.empty(sum(c["recv_cnts"]), dtype=dst.dtype, device=dst.device)
+    pack(kind, src, send, c["send_dist"], c["send_disp"])
+    if len(c["send_cnts"]) == 1:
+        recv.copy_(send)
+    else:
+        group = groups[1] if kind in (X_TO_Y, Y_TO_X) else groups[0]
+        k = 2 if send.is_complex() else 1
+        sv = torch.view_as_real(send).reshape(-1) if k == 2 else send
+        rv = torch.view_as_real(recv).reshape(-1) if k == 2 else recv
+        dist.all_to_all_single(rv, sv, [k * v for v in c["recv_cnts"]], [k * v for v in c["send_cnts"]],
+                               group=group)
+    unpack(kind, recv, dst, c["recv_dist"], c["recv_disp"])
+    return dst
+
+
+class DistFFT:
+    """3D FFT of an (nx, ny, nz) grid distributed over a p_row x p_col rank
+    grid, this rank's part: decomp_2d_fft_3d at p > 1 for the given
+    format (src/fft_common_3d.f90:9-296 with real transposes).
+
+    Each axis is transformed by an engine over the rank's pencil with the
+    other two axes skipped, and the pencils are exchanged by
+    transpose_dist: PHYSICAL_IN_X r2c = r2c along x on the X pencil,
+    x -> y, c2c along y, y -> z, c2c along z (the spectrum in Z pencils);
+    c2r the reverse; PHYSICAL_IN_Z the mirror image.  c2c runs the same
+    path on complex data.  Arrays are this rank's pencils (numpy view
+    (n3, n2, n1) of the Fortran sub-block), device tensors.
+
+    The *_steps methods are generators: they do the local work and yield
+    every transpose as (kind, src, dst, decomp) for the caller to perform;
+    r2c / c2r / c2c perform them with transpose_dist on `groups`
+    (pencil_groups(p_row, p_col); not needed on a 1 x 1 grid)."""
+
+    def __init__(self, fmt, nx, ny, nz, p_row, p_col, rank, prec=PREC_SINGLE, groups=None, device="cuda"):
+        import torch
+        if fmt not in (PHYSICAL_IN_X, PHYSICAL_IN_Z):
+            raise GbfftError(ERR_INVALID, "Invalid value for pencil")
+        self.fmt, self.prec, self.groups, self.device = fmt, prec, groups, device
+        self.ph = Decomp(nx, ny, nz, p_row, p_col, rank)
+        sp = (nx // 2 + 1, ny, nz) if fmt == PHYSICAL_IN_X else (nx, ny, nz // 2 + 1)
+        self.sp = Decomp(*sp, p_row, p_col, rank)
+        self.cdtype = torch.complex64 if prec == PREC_SINGLE else torch.complex128
+        self.rdtype = torch.float32 if prec == PREC_SINGLE else torch.float64
+
+        # one pass each, from its input to its output: no work area needed
+        # (a c2r input is still preserved)
+        def eng(f, sz, skip):
+            return Engine(f, sz[0], sz[1], sz[2], inplace=True, skip=skip, prec=prec)
+        x_only, y_only, z_only = (False, True, True), (True, False, True), (True, True, False)
+        if fmt == PHYSICAL_IN_X:
+            self.e_real = eng(PHYSICAL_IN_X, self.ph.xsz, x_only)  # r2c / c2r along x
+            self.e_last = eng(PHYSICAL_IN_X, self.sp.zsz, z_only)
+        else:
+            self.e_real = eng(PHYSICAL_IN_Z, self.ph.zsz, z_only)  # r2c / c2r along z
+            self.e_last = eng(PHYSICAL_IN_X, self.sp.xsz, x_only)
+        self.e_y = eng(PHYSICAL_IN_X, self.sp.ysz, y_only)
+        self._tmp = {}
+        self._cx = None
+
+    def _t(self, pencil, decomp=None):
+        d = decomp or self.sp
+        key = (pencil, id(d))
+        if key not in self._tmp:
+            import torch
+            self._tmp[key] = torch.empty(d.shape(pencil), dtype=self.cdtype, device=self.device)
+        return self._tmp[key]
+
+    def spectral_shape(self):
+        return self.sp.shape("z" if self.fmt == PHYSICAL_IN_X else "x")
+
+    def physical_shape(self):
+        return self.ph.shape("x" if self.fmt == PHYSICAL_IN_X else "z")
+
+    def r2c_steps(self, x, out):
+        first, last = ("x", "z") if self.fmt == PHYSICAL_IN_X else ("z", "x")
+        k1, k2 = (X_TO_Y, Y_TO_Z) if self.fmt == PHYSICAL_IN_X else (Z_TO_Y, Y_TO_X)
+        t1, ty = self._t(first), self._t("y")
+        self.e_real.r2c(x, t1)
+        yield (k1, t1, ty, self.sp)
+        self.e_y.c2c(ty, ty, FORWARD)
+        yield (k2, ty, out, self.sp)
+        self.e_last.c2c(out, out, FORWARD)
+
+    def c2r_steps(self, c, out):
+        """The input spectrum is preserved."""
+        first, last = ("x", "z") if self.fmt == PHYSICAL_IN_X else ("z", "x")
+        k1, k2 = (Z_TO_Y, Y_TO_X) if self.fmt == PHYSICAL_IN_X else (X_TO_Y, Y_TO_Z)
+        tl, ty, t1 = self._t(last), self._t("y"), self._t(first)
+        self.e_last.c2c(c, tl, BACKWARD)
+        yield (k1, tl, ty, self.sp)
+        self.e_y.c2c(ty, ty, BACKWARD)
+        yield (k2, ty, t1, self.sp)
+        self.e_real.c2r(t1, out)
+
+    def c2c_steps(self, a, out, isign):
+        """Complex data on the full grid: X pencil in, Z pencil out (forward,
+        PHYSICAL_IN_X) or the reverse, as src/fft_common_3d.f90:9-116."""
+        if self._cx is None:
+            def eng(sz, skip):
+                return Engine(PHYSICAL_IN_X, sz[0], sz[1], sz[2], inplace=True, skip=skip, prec=self.prec)
+            self._cx = {"x": eng(self.ph.xsz, (False, True, True)), "y": eng(self.ph.ysz, (True, False, True)),
+                        "z": eng(self.ph.zsz, (True, True, False))}
+        x_first = (self.fmt == PHYSICAL_IN_X) == (isign == FORWARD)
+        order = ("x", "y", "z") if x_first else ("z", "y", "x")
+        kinds = (X_TO_Y, Y_TO_Z) if x_first else (Z_TO_Y, Y_TO_X)
+        t0, ty = self._t(order[0], self.ph), self._t("y", self.ph)
+        self._cx[order[0]].c2c(a, t0, isign)
+        yield (kinds[0], t0, ty, self.ph)
+        self._cx["y"].c2c(ty, ty, isign)
+        yield (kinds[1], ty, out, self.ph)
+        self._cx[order[2]].c2c(out, out, isign)
+
+    def _drive(self, steps):
+        for kind, src, dst, decomp in steps:
+            transpose_dist(kind, src, dst, decomp, self.groups)
+
+    def r2c(self, x, out):
+        self._drive(self.r2c_steps(x, out))
+        return out
+
+    def c2r(self, c, out):
+        self._drive(self.c2r_steps(c, out))
+        return out
+
+    def c2c(self, a, out, isign):
+        self._drive(self.c2c_steps(a, out, isign))
+        return out
+
+    def close(self):
+        for e in [self.e_real, self.e_y, self.e_last] + (list(self._cx.values()) if self._cx else []):
+            e.close()

@@ -113,6 +113,71 @@ int gbfft_exec_c2c(gbfft_engine_t engine, void* d_in, void* d_out, int isign,
 int gbfft_transpose(int kind, int is_complex, int prec, const void* d_src,
                     void* d_dst, int n1, int n2, int n3, void* stream);
 
+/* ---- multi-rank pencil transposes (p_row x p_col ranks) ----------------
+ * The pieces of transpose_x_to_y / y_to_z / z_to_y / y_to_x on a
+ * p_row x p_col rank grid that run on each rank's GPU.  A transpose packs
+ * the local pencil into one send buffer of per-peer blocks
+ * (gbfft_transpose_pack), exchanges the buffers with the caller's
+ * communication library -- MPI_ALLTOALLV or NCCL grouped send/receive on the
+ * column communicator for x <-> y, the row communicator for y <-> z, as the
+ * reference does (src/transpose_x_to_y.f90:96-129,
+ * src/transpose_y_to_z.f90:94-156) -- and unpacks the received buffer into
+ * the destination pencil (gbfft_transpose_unpack).  Ranks are numbered
+ * row-major on the grid (rank = coord1 * p_col + coord2), as the
+ * reference's Cartesian topology (src/decomp_2d_init_fin.f90:95-122). */
+#define GBFFT_MAX_PEERS 1024 /* ranks of one row or column communicator */
+
+/* Sub-block of each pencil owned by a rank (1-based, inclusive ends):
+ * decomp_info_init's partition of the grid (src/decomp_2d.f90:411-416,
+ * partition :1016-1064), X pencil (x local, y over p_row, z over p_col),
+ * Y pencil (x over p_row, y local, z over p_col), Z pencil (x over p_row,
+ * y over p_col, z local). */
+typedef struct {
+  int xst[3], xen[3], xsz[3];
+  int yst[3], yen[3], ysz[3];
+  int zst[3], zen[3], zsz[3];
+  int coord[2]; /* (coord1, coord2) on the rank grid */
+} gbfft_pencil_info_t;
+/* Errors as the reference's: "Invalid 2D processor grid. Make sure that
+ * min(nx,ny) >= p_row and min(ny,nz) >= p_col" (src/decomp_2d.f90:399-405). */
+int gbfft_decomp_info(int nx, int ny, int nz, int p_row, int p_col, int rank, gbfft_pencil_info_t* info);
+/* distribute (src/decomp_2d.f90:1070-1105): n points over nproc ranks,
+ * 1-based starts, ends and sizes (nproc entries each). */
+int gbfft_decomp_distribute(int n, int nproc, int* st, int* en, int* sz);
+/* The exchange of one transpose kind (GBFFT_X_TO_Y ...) seen from `rank`:
+ * per peer of its communicator (*npeers = p_row for x <-> y, p_col for
+ * y <-> z, in communicator rank order), the block widths along the split
+ * dimension of the send side and of the receive side (the dist arrays of
+ * get_dist, src/decomp_2d.f90:1112-1133), and the ALLTOALLV send / receive
+ * counts and 0-based displacements in elements (prepare_buffer,
+ * :1138-1206).  Arrays of GBFFT_MAX_PEERS entries are always large enough. */
+int gbfft_decomp_counts(int nx, int ny, int nz, int p_row, int p_col, int rank, int kind, int* send_dist,
+                        int* send_cnts, int* send_disp, int* recv_dist, int* recv_cnts, int* recv_disp,
+                        int* npeers);
+/* mem_split_* of a transpose kind as one kernel: the local (n1, n2, n3)
+ * source pencil (real or complex, single or double precision) split along
+ * the kind's send dimension (x for X_TO_Y, y for Y_TO_Z and Y_TO_X, z for
+ * Z_TO_Y) into npeers blocks of widths dist[m], block m written in Fortran
+ * order at element displacement disp[m] of d_send
+ * (src/transpose_x_to_y.f90:266-323, src/transpose_y_to_z.f90:370-428,
+ * src/transpose_z_to_y.f90:370-427, src/transpose_y_to_x.f90:266-323).
+ * dist and disp are host arrays; the copy is bit-exact and stream-ordered.
+ * send_elems is the send buffer's size in elements: a block that would reach
+ * past it is rejected (GBFFT_ERR_INVALID) before anything is launched. */
+int gbfft_transpose_pack(int kind, int is_complex, int prec, const void* d_src, int n1, int n2, int n3,
+                         int npeers, const int* dist, const int* disp, void* d_send, size_t send_elems,
+                         void* stream);
+/* mem_merge_* of a transpose kind as one kernel: the received blocks of
+ * d_recv (widths dist[m] along the kind's receive dimension -- y for X_TO_Y
+ * and Z_TO_Y, z for Y_TO_Z, x for Y_TO_X -- at displacements disp[m]) into
+ * the local (n1, n2, n3) destination pencil (src/transpose_x_to_y.f90:384-441,
+ * src/transpose_y_to_z.f90:490-548, src/transpose_z_to_y.f90:488-545,
+ * src/transpose_y_to_x.f90:384-441).  recv_elems: d_recv's size in
+ * elements, checked as for the pack. */
+int gbfft_transpose_unpack(int kind, int is_complex, int prec, const void* d_recv, int n1, int n2, int n3,
+                           int npeers, const int* dist, const int* disp, size_t recv_elems, void* d_dst,
+                           void* stream);
+
 /* Device memory for pencil arrays: replaces alloc_x/alloc_y/alloc_z of the
  * device build (src/alloc_dev.f90:10-135).  gbfft_malloc returns 256-byte
  * aligned memory. */
