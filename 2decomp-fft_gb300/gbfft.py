@@ -53,6 +53,7 @@ SIGNATURES = {
     "gbfft_decomp_counts": (_i, [_i] * 7 + [_ip] * 7),
     "gbfft_transpose_pack": (_i, [_i, _i, _i, _vp, _i, _i, _i, _i, _ip, _ip, _vp, _sz, _vp]),
     "gbfft_transpose_unpack": (_i, [_i, _i, _i, _vp, _i, _i, _i, _i, _ip, _ip, _sz, _vp, _vp]),
+    "gbfft_box_copy": (_i, [_i, _i, _vp, _ip, _ip, _vp, _ip, _ip, _ip, _vp]),
     "gbfft_free": (_i, [_vp]),
     "gbfft_last_error_string": (ctypes.c_char_p, []),
     "gbfft_warning_count": (_i, []),
@@ -813,3 +814,142 @@ class DistFFT:
     def close(self):
         for e in [self.e_real, self.e_y, self.e_last] + (list(self._cx.values()) if self._cx else []):
             e.close()
+
+
+# ---------------------------------------------------------------------------
+# halo-cell update (src/halo.f90, src/halo_common.f90)
+# ---------------------------------------------------------------------------
+HALO_PHASES = {"x": (1, 2), "y": (0, 2), "z": (0, 1)}  # distributed axes, phase order
+
+
+def box_copy(src, src_off, dst, dst_off, box, stream=None):
+    """gbfft_box_copy: the Fortran box `box` = (w1, w2, w3) of `src` at
+    src_off into `dst` at dst_off (0-based offsets; tensors viewed
+    (n3, n2, n1), same dtype, on the device)."""
+    cplx, prec = _elem(src)
+    sd = src.shape[::-1]
+    dd = dst.shape[::-1]
+    check(lib().gbfft_box_copy(int(cplx), prec, _ptr(src), _int3(sd), _int3(src_off), _ptr(dst), _int3(dd),
+                               _int3(dst_off), _int3(box), _stream(stream)))
+    return dst
+
+
+def halo_extents(pencil, sizes, level, start=None):
+    """Index ranges (1-based, inclusive, Fortran order) of the halo-extended
+    array of a pencil of local sizes (s1, s2, s3): init_halo_extents of
+    src/halo.f90:230-309.  With `start` (the pencil's xst / yst / zst) the
+    global-coordinate form (opt_global)."""
+    st = list(start) if start is not None else [1, 1, 1]
+    lo, hi = [], []
+    for d in range(3):
+        l = level if d in HALO_PHASES[pencil] else 0
+        lo.append(st[d] - l)
+        hi.append(st[d] + sizes[d] - 1 + l)
+    return lo, hi
+
+
+def _halo_neighbours(coord, dims, cdim, periodic):
+    me = coord[cdim]
+
+    def nb(shift):
+        c = list(coord)
+        v = me + shift
+        if v < 0 or v >= dims[cdim]:
+            if not periodic:
+                return None
+            v %= dims[cdim]
+        c[cdim] = v
+        return c[0] * dims[1] + c[1]
+    return nb(-1), nb(+1)
+
+
+def update_halo(inp, level, decomp, pencil, periodic=(False, False, False), copy=None, exchange=None):
+    """update_halo (src/halo.f90:100-146 with src/halo_common.f90): a new
+    array holding this rank's pencil `inp` with `level` halo cells on the
+    pencil's two distributed axes, filled from the neighbouring ranks of the
+    p_row x p_col grid of `decomp` (rank, coordinates, grid).  periodic =
+    (periodic_x, periodic_y, periodic_z) of decomp_2d_init.
+
+    As the reference: the halos are filled in two phases (X pencil: y then
+    z, Y pencil: x then z, Z pencil: x then y), each moving slabs that span
+    the whole halo-extended array in the other axes, so the corners come
+    from diagonal neighbours; across a non-periodic edge a halo is left as
+    allocated (unset); on a periodic dimension of one rank the rank is its
+    own neighbour and, as the reference's two same-tag messages match, its
+    low halo receives its own first interior planes and its high halo its
+    last ones.
+
+    Device work: one box copy into the interior, box copies packing and
+    unpacking the slabs (gbfft_box_copy); the exchange: torch.distributed
+    point-to-point in two batches per phase (every rank's minus-going
+    messages, then its plus-going ones), so that a pair of ranks that are
+    each other's two neighbours never has two messages in flight the same
+    way.  `copy` / `exchange` replace the device copy and the exchange
+    (tests)."""
+    import torch
+    copy = copy or box_copy
+    sizes = list(inp.shape[::-1])
+    if pencil not in HALO_PHASES:
+        raise GbfftError(ERR_INVALID, "Invalid data passed to update_halo")
+    for a in HALO_PHASES[pencil]:
+        if level < 0 or sizes[a] < level:
+            raise GbfftError(ERR_INVALID, "halo level larger than the local pencil")
+    ext = list(sizes)
+    for a in HALO_PHASES[pencil]:
+        ext[a] += 2 * level
+    out = torch.empty(ext[::-1], dtype=inp.dtype, device=inp.device)
+    off = [level if d in HALO_PHASES[pencil] else 0 for d in range(3)]
+    copy(inp, [0, 0, 0], out, off, sizes)
+    if level == 0:
+        return out
+    dims = (decomp.p_row, decomp.p_col)
+    for phase, axis in enumerate(HALO_PHASES[pencil]):
+        minus, plus = _halo_neighbours(decomp.coord, dims, phase, periodic[axis])
+        s = sizes[axis]
+        box = list(ext)
+        box[axis] = level
+
+        def at(pos):
+            o = [0, 0, 0]
+            o[axis] = pos
+            return o
+        me = decomp.rank
+        # the rank its own neighbour (one rank on a periodic dimension): the
+        # reference's matching gives each halo the adjacent interior planes
+        if minus == me and plus == me:
+            copy(out, at(level), out, at(0), box)
+            copy(out, at(s), out, at(s + level), box)
+            continue
+        def slab(pos):
+            b = torch.empty(box[::-1], dtype=out.dtype, device=out.device)
+            copy(out, at(pos), b, [0, 0, 0], box)
+            return b
+        # minus-going: own first interior planes to minus, high halo from plus
+        # plus-going: own last interior planes to plus, low halo from minus
+        send_lo = slab(level) if minus is not None else None
+        send_hi = slab(s) if plus is not None else None
+        recv_hi = torch.empty(box[::-1], dtype=out.dtype, device=out.device) if plus is not None else None
+        recv_lo = torch.empty(box[::-1], dtype=out.dtype, device=out.device) if minus is not None else None
+        (exchange or _p2p)([(send_lo, minus)], [(recv_hi, plus)])
+        (exchange or _p2p)([(send_hi, plus)], [(recv_lo, minus)])
+        if recv_hi is not None:
+            copy(recv_hi, [0, 0, 0], out, at(s + level), box)
+        if recv_lo is not None:
+            copy(recv_lo, [0, 0, 0], out, at(0), box)
+    return out
+
+
+def _p2p(sends, recvs):
+    """One batch of point-to-point messages (torch.distributed)."""
+    import torch
+    import torch.distributed as dist
+    ops = []
+    for t, peer in sends:
+        if t is not None and peer is not None:
+            ops.append(dist.P2POp(dist.isend, torch.view_as_real(t) if t.is_complex() else t, peer))
+    for t, peer in recvs:
+        if t is not None and peer is not None:
+            ops.append(dist.P2POp(dist.irecv, torch.view_as_real(t) if t.is_complex() else t, peer))
+    if ops:
+        for req in dist.batch_isend_irecv(ops):
+            req.wait()

@@ -178,6 +178,20 @@ int gbfft_transpose_unpack(int kind, int is_complex, int prec, const void* d_rec
                            int npeers, const int* dist, const int* disp, size_t recv_elems, void* d_dst,
                            void* stream);
 
+/* ---- halo-cell update (src/halo.f90, src/halo_common.f90) -------------
+ * The device data movement of update_halo: a copy of the box of
+ * box[0] x box[1] x box[2] elements at 0-based offset src_off of the
+ * Fortran-ordered array d_src (extents src_dims) to dst_off of d_dst
+ * (extents dst_dims) -- the pencil into the interior of its halo-extended
+ * array (src/halo_common.f90:20-75), and the slabs of `level` planes a rank
+ * sends to and receives from its neighbours, packed into and unpacked from
+ * contiguous buffers (halo_exchange_{x,y,z}_body.f90; the exchange itself
+ * is the caller's point-to-point messaging, as MPI_IRECV / MPI_ISSEND
+ * there).  Bit-exact, stream-ordered; a box outside either array is
+ * rejected (GBFFT_ERR_INVALID) before anything is launched. */
+int gbfft_box_copy(int is_complex, int prec, const void* d_src, const int* src_dims, const int* src_off,
+                   void* d_dst, const int* dst_dims, const int* dst_off, const int* box, void* stream);
+
 /* Device memory for pencil arrays: replaces alloc_x/alloc_y/alloc_z of the
  * device build (src/alloc_dev.f90:10-135).  gbfft_malloc returns 256-byte
  * aligned memory. */
