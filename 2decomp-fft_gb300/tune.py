@@ -45,6 +45,8 @@ DEFAULT_SHAPES = [
     (4, 1, 384, 400, 243), (8, 1, 384, 400, 243),
     (4, 1, 360, 270, 210), (8, 1, 360, 270, 210),
     (4, 1, 256, 256, 256), (8, 1, 64, 64, 64),
+    # reduced grids of the 1024 x 1024 x 512 passes, for profiling
+    (4, 1, 1024, 1024, 128), (4, 1, 512, 256, 512),
 ]
 TILES = [1, 2, 4, 8, 16, 32]
 MARGIN = 0.99

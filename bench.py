@@ -45,8 +45,10 @@ WORKLOADS = {
     "r2c_c2r_360x270x210_f64_x": (360, 270, 210, 1, 8, "uniform"),
     "r2c_c2r_360x270x210_f32_x": (360, 270, 210, 1, 4, "uniform"),
     "r2c_c2r_256x256x256_f32_x": (256, 256, 256, 1, 4, "uniform"),
-    # profiling sizes: the x/y lines of the 1024x1024x512 grid at ~1/4 the memory
+    # profiling sizes: the x/y lines of the 1024x1024x512 grid at ~1/4 the memory,
+    # its 512-point z lines (flat planes of 257-value rows) at ~1/8
     "r2c_c2r_1024x1024x128_f32_x": (1024, 1024, 128, 1, 4, "gauss_modes"),
+    "r2c_c2r_512x256x512_f32_x": (512, 256, 512, 1, 4, "gauss_modes"),
     "r2c_c2r_1024x64x512_f32_x": (1024, 64, 512, 1, 4, "gauss_modes"),
 }
 DEFAULT_WORKLOAD = "r2c_c2r_1024x1024x512_f32_x"
@@ -488,6 +490,8 @@ def run_gb300(args):
         roof = {"bound": "hbm", "kernel": "axis pass %s" % dom, "achieved": round(d["gbs"], 1),
                 "peak": peak, "unit": "GB/s", "frac": round(d["gbs"] / peak, 4),
                 "traffic": read_traffic(args.workload + ("" if args.form == "plain" else ":" + args.form), dom),
+                "traffic_source": "committed profile (profiles/dram_traffic.txt: ncu dram bytes of reduced grids "
+                                  "of the same kernel, scaled to a full launch), not measured in this run",
                 "peak_source": peak_src,
                 "step_frac": round(algo_bytes_step / (ms_max * 1e-3) / 1e9 / peak, 4)}
 
