@@ -41,8 +41,20 @@ def _newest_input():
     return max(os.path.getmtime(f) for f in files)
 
 
-def _compile(src, extra):
-    obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+def paths(variant=""):
+    """(object directory, library path) of a build variant: "" the product
+    library lib/libgbfft.so, "debug" the bounds-checked build
+    lib/debug/libgbfft.so (-DGB_DEBUG_BOUNDS)."""
+    if not variant:
+        return OBJ, LIB
+    return os.path.join(HERE, "lib", "obj_" + variant), os.path.join(HERE, "lib", variant, "libgbfft.so")
+
+
+VARIANT_FLAGS = {"": [], "debug": ["-DGB_DEBUG_BOUNDS"]}
+
+
+def _compile(src, extra, obj_dir=OBJ):
+    obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
     cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd[1:1] = ["-x", "cu"]
@@ -52,27 +64,32 @@ def _compile(src, extra):
     return obj, r.stderr
 
 
-def build(force=False, verbose=False, extra=()):
-    """Compile and link the library if any input is newer; return its path."""
-    os.makedirs(OBJ, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_input():
-        return LIB
+def build(force=False, verbose=False, extra=(), variant=""):
+    """Compile and link the library (or a variant of it) if any input is
+    newer; return its path."""
+    obj_dir, lib_path = paths(variant)
+    os.makedirs(obj_dir, exist_ok=True)
+    os.makedirs(os.path.dirname(lib_path), exist_ok=True)
+    if not force and os.path.exists(lib_path) and os.path.getmtime(lib_path) >= _newest_input():
+        return lib_path
     srcs = sources()
+    flags = list(extra) + VARIANT_FLAGS[variant]
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        results = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
+        results = list(ex.map(lambda s: _compile(s, flags, obj_dir), srcs))
     if verbose:
         for _, log in results:
             if log.strip():
                 print(log)
-    tmp = LIB + ".tmp.%d" % os.getpid()
+    tmp = lib_path + ".tmp.%d" % os.getpid()
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results] + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
     extra = [a for a in sys.argv[1:] if a.startswith("-X") or a.startswith("-D")]
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, extra=extra))
+    variant = sys.argv[sys.argv.index("--variant") + 1] if "--variant" in sys.argv else ""
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, extra=extra, variant=variant))

@@ -53,9 +53,9 @@ void drop_graph(gbfft_batch_t b) {
 }
 
 void drop_desc(gbfft_batch_t b) {
-  if (b->d_desc) cudaFree(b->d_desc);
-  if (b->d_prefix) cudaFree(b->d_prefix);
-  if (b->d_sync) cudaFree(b->d_sync);
+  if (b->d_desc) dev_free(b->d_desc);
+  if (b->d_prefix) dev_free(b->d_prefix);
+  if (b->d_sync) dev_free(b->d_sync);
   b->d_desc = nullptr;
   b->d_prefix = nullptr;
   b->d_sync = nullptr;
@@ -133,9 +133,9 @@ int build_desc(gbfft_batch_t b, int mask) {
       prefix.push_back(prefix.back() + (d.lines + le - 1) / le);
     }
   b->ndesc = (int)desc.size();
-  cudaError_t e = cudaMalloc(&b->d_desc, desc.size() * sizeof(BatchDesc));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_prefix, prefix.size() * sizeof(long long));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_sync, (desc.size() + 2) * sizeof(int));
+  cudaError_t e = dev_malloc((void**)&b->d_desc, desc.size() * sizeof(BatchDesc));
+  if (e == cudaSuccess) e = dev_malloc((void**)&b->d_prefix, prefix.size() * sizeof(long long));
+  if (e == cudaSuccess) e = dev_malloc((void**)&b->d_sync, (desc.size() + 2) * sizeof(int));
   if (e == cudaSuccess)
     e = cudaMemcpy(b->d_desc, desc.data(), desc.size() * sizeof(BatchDesc), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)

@@ -13,6 +13,7 @@
 //   c2r:  in -> W -> W -> out, W = in when inplace, else the engine's work
 //         area (the complex intermediate does not fit in the real output).
 #include <dlfcn.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cmath>
@@ -35,6 +36,33 @@ namespace {
 
 thread_local std::string g_err;
 std::atomic<int> g_warnings{0};
+// gbfft_debug_fail_alloc: allocations to let through before one fails (-1:
+// none fails)
+std::atomic<long long> g_fail_alloc{-1};
+// NVTX ranges around transforms and passes (gbfft_set_nvtx, GBFFT_NVTX=1)
+std::atomic<int> g_nvtx{-1};
+bool nvtx_on() {
+  int v = g_nvtx.load();
+  if (v < 0) {
+    const char* env = std::getenv("GBFFT_NVTX");
+    v = (env && env[0] && env[0] != '0') ? 1 : 0;
+    g_nvtx.store(v);
+  }
+  return v == 1;
+}
+// a named range of the transform (the reference's profiler regions
+// "fft_r2c" / "fft_c2r" / "fft_c2c", src/fft_common_3d.f90:22,114) or pass
+struct Range {
+  bool on;
+  explicit Range(const char* name) : on(nvtx_on()) {
+    if (on) nvtxRangePushA(name);
+  }
+  ~Range() {
+    if (on) nvtxRangePop();
+  }
+};
+const char* kPassNames[GBFFT_PASS_KINDS] = {"pass r2c", "pass c2r", "pass c2c x", "pass c2c y", "pass c2c z",
+                                            "pass x+y fused"};
 
 int fail(int code, const std::string& msg) {
   g_err = msg;
@@ -151,10 +179,10 @@ std::vector<double> stage_twiddles(const std::vector<int>& radices) {
 
 int upload_table(void** dst, const std::vector<double>& t, int prec) {
   const size_t bytes = t.size() / 2 * 2 * (size_t)prec;
-  cudaError_t e = cudaMalloc(dst, bytes);
+  cudaError_t e = dev_malloc(dst, bytes);
   if (e != cudaSuccess) {
     *dst = nullptr;
-    return cuda_fail(e, "cudaMalloc(twiddles)");
+    return fail(GBFFT_ERR_ALLOC, std::string("cudaMalloc(twiddles): ") + cudaGetErrorString(e));
   }
   if (prec == 8) {
     e = cudaMemcpy(*dst, t.data(), bytes, cudaMemcpyHostToDevice);
@@ -335,18 +363,18 @@ void drop_profile(gbfft_engine_t e) {
 void release(gbfft_engine_t e) {
   drop_profile(e);
   for (auto& a : e->ax) {
-    if (a.d_tw) cudaFree(a.d_tw);
-    if (a.d_twf) cudaFree(a.d_twf);
+    if (a.d_tw) dev_free(a.d_tw);
+    if (a.d_twf) dev_free(a.d_twf);
     a.d_tw = nullptr;
     a.d_twf = nullptr;
   }
-  if (e->work) cudaFree(e->work);
+  if (e->work) dev_free(e->work);
   e->work = nullptr;
-  if (e->d_sync) cudaFree(e->d_sync);
+  if (e->d_sync) dev_free(e->d_sync);
   e->d_sync = nullptr;
-  if (e->d_status) cudaFree(e->d_status);
+  if (e->d_status) dev_free(e->d_status);
   e->d_status = nullptr;
-  if (e->long_scratch) cudaFree(e->long_scratch);
+  if (e->long_scratch) dev_free(e->long_scratch);
   e->long_scratch = nullptr;
 }
 
@@ -739,8 +767,29 @@ void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
   }
 }
 
-int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st) {
-  for (const Pass& p : ps) {
+// Arrays of one transform (base, bytes), for the extents the bounds-checked
+// build checks every access against.
+struct Extent {
+  const void* p;
+  size_t bytes;
+};
+
+int run_passes(gbfft_engine_s* e, const std::vector<Pass>& ps, cudaStream_t st,
+               std::initializer_list<Extent> arrays = {}) {
+  for (const Pass& pc : ps) {
+    Pass p = pc;
+    // every pass reports to the engine's status word; the checked build
+    // also needs each side's extent in elements of that side's type
+    if (!p.a.status) p.a.status = e->d_status;
+    const size_t cb = cbytes(e), rb = (size_t)e->prec;
+    const size_t se = p.kind == K_R2C ? rb : cb, de = p.kind == K_C2R ? rb : cb;
+    for (const Extent& x : arrays) {
+      if (x.p == p.a.src) p.a.src_elems = (long long)(x.bytes / se);
+      if (x.p == p.a.dst) p.a.dst_elems = (long long)(x.bytes / de);
+    }
+    if (e->work == p.a.src) p.a.src_elems = (long long)(e->work_bytes / se);
+    if (e->work == p.a.dst) p.a.dst_elems = (long long)(e->work_bytes / de);
+    Range range(p.fused ? "pass x+y fused" : kPassNames[p.prof_kind]);
     ProfRec rec{p.prof_kind, nullptr, nullptr, p.bytes};
     if (e->profiling) {
       if (cudaEventCreate(&rec.start) != cudaSuccess || cudaEventCreate(&rec.stop) != cudaSuccess)
@@ -942,6 +991,34 @@ int gbfft::engine_passes(gbfft_engine_s* e, int which, const void* in, void* out
 
 int gbfft::engine_precision(gbfft_engine_s* e) { return valid_engine(e) ? e->prec : 0; }
 
+std::atomic<long long> g_live_allocs{0};
+
+cudaError_t gbfft::dev_free(void* p) {
+  if (!p) return cudaSuccess;
+  cudaError_t e = cudaFree(p);
+  if (e == cudaSuccess) g_live_allocs.fetch_sub(1);
+  return e;
+}
+
+long long gbfft_debug_live_allocations(void) { return g_live_allocs.load(); }
+
+cudaError_t gbfft::dev_malloc(void** p, size_t bytes) {
+  long long v = g_fail_alloc.load();
+  while (v >= 0) {
+    const long long next = v == 0 ? -1 : v - 1;
+    if (g_fail_alloc.compare_exchange_weak(v, next)) {
+      if (v == 0) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+      }
+      break;
+    }
+  }
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) g_live_allocs.fetch_add(1);
+  return e;
+}
+
 int gbfft::set_error(int code, const char* msg) {
   g_err = msg ? msg : "";
   return code;
@@ -966,11 +1043,30 @@ long long gbfft_launch_count(void) { return launch_counter(); }
 
 long long gbfft_tma_pass_count(void) { return tma_launch_counter(); }
 
+int gbfft_debug_fail_alloc(long long nth) {
+  if (nth < -1) return fail(GBFFT_ERR_INVALID, "bad argument");
+  g_fail_alloc.store(nth);
+  return GBFFT_OK;
+}
+
+int gbfft_set_nvtx(int enable) {
+  g_nvtx.store(enable ? 1 : 0);
+  return GBFFT_OK;
+}
+
+int gbfft_debug_bounds_build(void) {
+#ifdef GB_DEBUG_BOUNDS
+  return 1;
+#else
+  return 0;
+#endif
+}
+
 int gbfft_malloc(void** d_ptr, size_t bytes) {
   if (!d_ptr) return fail(GBFFT_ERR_INVALID, "gbfft_malloc: null output pointer");
   *d_ptr = nullptr;
   if (bytes == 0) return GBFFT_OK;
-  cudaError_t e = cudaMalloc(d_ptr, bytes);
+  cudaError_t e = dev_malloc(d_ptr, bytes);
   if (e != cudaSuccess) {
     *d_ptr = nullptr;
     g_err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
@@ -981,7 +1077,7 @@ int gbfft_malloc(void** d_ptr, size_t bytes) {
 
 int gbfft_free(void* d_ptr) {
   if (!d_ptr) return GBFFT_OK;
-  cudaError_t e = cudaFree(d_ptr);
+  cudaError_t e = dev_free(d_ptr);
   if (e != cudaSuccess) return cuda_fail(e, "cudaFree");
   return GBFFT_OK;
 }
@@ -1012,7 +1108,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
   // unless the transforms must work in the arrays they are given
   if (!e->inplace) {
     e->work_bytes = (size_t)padded_pitch(e) * e->sp[1] * e->sp[2] * cbytes(e);
-    cudaError_t err = cudaMalloc(&e->work, e->work_bytes);
+    cudaError_t err = dev_malloc(&e->work, e->work_bytes);
     if (err != cudaSuccess) {
       e->work = nullptr;
       release(e);
@@ -1024,7 +1120,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
   // counters of the fused x/y kernel: one per z-plane plus ticket and status
   if (prec == GBFFT_PREC_SINGLE && fast_length(nx) && fast_length(ny)) {
     e->sync_planes = nz;
-    cudaError_t err = cudaMalloc(&e->d_sync, (size_t)(nz + 2) * sizeof(int));
+    cudaError_t err = dev_malloc((void**)&e->d_sync, (size_t)(nz + 2) * sizeof(int));
     if (err != cudaSuccess) {
       e->d_sync = nullptr;
       release(e);
@@ -1035,7 +1131,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
     cudaMemset(e->d_sync, 0, (size_t)(nz + 2) * sizeof(int));
   }
   {
-    cudaError_t err = cudaMalloc(&e->d_status, 4 * sizeof(int));
+    cudaError_t err = dev_malloc((void**)&e->d_status, 4 * sizeof(int));
     if (err != cudaSuccess) {
       e->d_status = nullptr;
       release(e);
@@ -1049,7 +1145,7 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
   // at most the whole grid in complex values (any engine may run c2c)
   if (e->ax[0].big || e->ax[1].big || e->ax[2].big) {
     e->long_scratch_bytes = 2 * (size_t)nx * ny * nz * cbytes(e);
-    cudaError_t err = cudaMalloc(&e->long_scratch, e->long_scratch_bytes);
+    cudaError_t err = dev_malloc(&e->long_scratch, e->long_scratch_bytes);
     if (err != cudaSuccess) {
       e->long_scratch = nullptr;
       release(e);
@@ -1100,9 +1196,10 @@ int gbfft_exec_r2c(gbfft_engine_t e, const void* d_in, void* d_out, void* stream
   cudaStream_t st = (cudaStream_t)stream;
   if ((e->format == GBFFT_PHYSICAL_IN_X && e->skip[0]) || (e->format == GBFFT_PHYSICAL_IN_Z && e->skip[2]))
     warn_skip(e->format == GBFFT_PHYSICAL_IN_X ? 1 : 2);
+  Range range("fft_r2c");
   std::vector<Pass> ps = r2c_passes(e, d_in, d_out);
   if (e->fuse) fuse_xy(e, ps, e->sp[2]);
-  return run_passes(e, ps, st);
+  return run_passes(e, ps, st, {{d_in, rb}, {d_out, cb}});
 }
 
 int gbfft_exec_c2r(gbfft_engine_t e, void* d_in, void* d_out, void* stream) {
@@ -1118,9 +1215,10 @@ int gbfft_exec_c2r(gbfft_engine_t e, void* d_in, void* d_out, void* stream) {
   if (!(e->inplace ? d_in : e->work)) return fail(GBFFT_ERR_STATE, "engine has no work area");
   if (e->format == GBFFT_PHYSICAL_IN_X && e->skip[0]) warn_skip(3);
   if (e->format == GBFFT_PHYSICAL_IN_Z && e->skip[2]) warn_skip(4);
+  Range range("fft_c2r");
   std::vector<Pass> ps = c2r_passes(e, d_in, d_out);
   if (e->fuse) fuse_xy(e, ps, e->sp[2]);
-  return run_passes(e, ps, st);
+  return run_passes(e, ps, st, {{d_in, cb}, {d_out, rb}});
 }
 
 int gbfft_exec_c2c(gbfft_engine_t e, void* d_in, void* d_out, int isign, void* stream) {
@@ -1135,6 +1233,7 @@ int gbfft_exec_c2c(gbfft_engine_t e, void* d_in, void* d_out, int isign, void* s
     return fail(GBFFT_ERR_INVALID, "input and output partially overlap");
   if (!aligned(d_in, cbytes(e)) || !aligned(d_out, cbytes(e)))
     return fail(GBFFT_ERR_INVALID, "array not aligned to its element size");
+  Range range("fft_c2c");
   std::vector<Pass> ps = c2c_passes(e, d_in, d_out, isign);
   if (ps.empty()) {
     cudaError_t err = launch_copy(d_in, d_out, bytes, st);
@@ -1142,7 +1241,7 @@ int gbfft_exec_c2c(gbfft_engine_t e, void* d_in, void* d_out, int isign, void* s
     return GBFFT_OK;
   }
   if (e->fuse) fuse_xy(e, ps, n3);
-  return run_passes(e, ps, st);
+  return run_passes(e, ps, st, {{d_in, bytes}, {d_out, bytes}});
 }
 
 int gbfft_transpose(int kind, int is_complex, int prec, const void* d_src, void* d_dst, int n1, int n2,
@@ -1259,6 +1358,7 @@ int gbfft_engine_status(gbfft_engine_t e) {
   if (e->d_status) {
     cudaError_t err = cudaMemcpy(&flag, e->d_status, sizeof(int), cudaMemcpyDeviceToHost);
     if (err != cudaSuccess) return cuda_fail(err, "cudaMemcpy(status)");
+    if (flag == 2) return fail(GBFFT_ERR_BOUNDS, "a bounds check caught an access outside its array (skipped)");
     if (flag) return fail(GBFFT_ERR_TIMEOUT, "a pass gave up waiting for its bulk tensor copies");
   }
   if (!e->d_sync) return GBFFT_OK;
@@ -1283,13 +1383,13 @@ int gbfft_engine_get_tma(gbfft_engine_t e, int* enable) {
 int gbfft_selftest_bounded_wait(int counter_value, int need, long long poll_limit, int* timed_out) {
   if (!timed_out || poll_limit < 1 || poll_limit > (1ll << 26)) return fail(GBFFT_ERR_INVALID, "bad argument");
   int* d = nullptr;
-  cudaError_t err = cudaMalloc(&d, 2 * sizeof(int));
+  cudaError_t err = dev_malloc((void**)&d, 2 * sizeof(int));
   if (err != cudaSuccess) return cuda_fail(err, "cudaMalloc");
   int h[2] = {counter_value, 0};
   err = cudaMemcpy(d, h, sizeof h, cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = launch_wait_selftest(d, need, poll_limit, nullptr);
   if (err == cudaSuccess) err = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
-  cudaFree(d);
+  dev_free(d);
   if (err != cudaSuccess) return cuda_fail(err, "bounded-wait self-test");
   *timed_out = h[1];
   return GBFFT_OK;
@@ -1328,7 +1428,7 @@ int gbfft_engine_set_plan(gbfft_engine_t e, int axis, int points) {
     return rc;
   }
   cudaDeviceSynchronize();  // no pass still reads the old table
-  if (old) cudaFree(old);
+  if (old) dev_free(old);
   for (int k = 0; k < GBFFT_PASS_KINDS; ++k) e->tile_L[k] = 0;  // tiles were sized for the old plan
   return GBFFT_OK;
 }
@@ -1473,9 +1573,9 @@ bool valid_dtt(gbfft_dtt_t d) { return d != nullptr && d->magic == kDttMagic; }
 void release_dtt(gbfft_dtt_t d) {
   for (auto& dir : d->ax)
     for (DttAxis& a : dir) {
-      if (a.tw) cudaFree(a.tw);
-      if (a.twf) cudaFree(a.twf);
-      if (a.w4) cudaFree(a.w4);
+      if (a.tw) dev_free(a.tw);
+      if (a.twf) dev_free(a.twf);
+      if (a.w4) dev_free(a.w4);
       a.tw = a.twf = a.w4 = nullptr;
     }
 }

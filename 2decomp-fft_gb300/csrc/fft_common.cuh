@@ -396,6 +396,23 @@ struct LineCtx {
   long long sb0, sb1, db0, db1, ssn, dsn;
   int N, L, tpl, t, line;
   bool valid, has1, inverse, pvec, cvec;
+#ifdef GB_DEBUG_BOUNDS
+  // bounds-checked build: every global access is checked against the
+  // array's extent; one outside it records 2 in the status word and is
+  // skipped (a load reads zero)
+  long long se, de;
+  int* st;
+  __device__ __forceinline__ bool ok(long long off, int w, long long n) const {
+    if (off >= 0 && off + w <= n) return true;
+    if (st) atomicExch(st, 2);
+    return false;
+  }
+#define GB_SRC(off, w) ok((off), (w), se)
+#define GB_DST(off, w) ok((off), (w), de)
+#else
+#define GB_SRC(off, w) true
+#define GB_DST(off, w) true
+#endif
 
   __device__ __forceinline__ void init(const PassArgs& a) {
     if (CONTIG)
@@ -419,6 +436,11 @@ struct LineCtx {
     inverse = a.inverse != 0;
     ssn = a.s_src_n;
     dsn = a.s_dst_n;
+#ifdef GB_DEBUG_BOUNDS
+    se = a.src_elems;
+    de = a.dst_elems;
+    st = a.status;
+#endif
     pvec = !CONTIG && (a.pair_vec & 1);
     cvec = !CONTIG && std::is_same<T, float>::value && (a.pair_vec & 2);
     t = t_;
@@ -515,22 +537,26 @@ struct LineCtx {
   __device__ __forceinline__ C gload(int n) const {
     if (PRED && !valid) return cmk<C>(T(0), T(0));
     if (KIND == K_C2C) {
+      if (!GB_SRC(sb0 + n * ssn, 1)) return cmk<C>(T(0), T(0));
       C x = ld(reinterpret_cast<const C*>(src) + sb0 + n * ssn);
       if (inverse) x.y = -x.y;
       return x;
     } else if (KIND == K_R2C) {
       const T* s = reinterpret_cast<const T*>(src);
-      if (!CONTIG && pvec && has1) return ld(reinterpret_cast<const C*>(s + sb0 + n * ssn));
-      const T re = ld(s + sb0 + n * ssn);
-      const T im = has1 ? ld(s + sb1 + n * ssn) : T(0);
+      if (!CONTIG && pvec && has1) {
+        if (!GB_SRC(sb0 + n * ssn, 2)) return cmk<C>(T(0), T(0));
+        return ld(reinterpret_cast<const C*>(s + sb0 + n * ssn));
+      }
+      const T re = GB_SRC(sb0 + n * ssn, 1) ? ld(s + sb0 + n * ssn) : T(0);
+      const T im = (has1 && GB_SRC(sb1 + n * ssn, 1)) ? ld(s + sb1 + n * ssn) : T(0);
       return cmk<C>(re, im);
     } else {
       // Hermitian extension of both half spectra (src/fft_generic.f90:318-330)
       const C* s = reinterpret_cast<const C*>(src);
       const bool low = 2 * n <= N;
       const int m = low ? n : N - n;
-      C x1 = ld(s + sb0 + m * ssn);
-      C x2 = has1 ? ld(s + sb1 + m * ssn) : cmk<C>(T(0), T(0));
+      C x1 = GB_SRC(sb0 + m * ssn, 1) ? ld(s + sb0 + m * ssn) : cmk<C>(T(0), T(0));
+      C x2 = (has1 && GB_SRC(sb1 + m * ssn, 1)) ? ld(s + sb1 + m * ssn) : cmk<C>(T(0), T(0));
       if (!low) {
         x1.y = -x1.y;
         x2.y = -x2.y;
@@ -556,15 +582,15 @@ struct LineCtx {
     if (!valid) return;
     if (KIND == K_C2C) {
       if (inverse) v.y = -v.y;
-      reinterpret_cast<C*>(dst)[db0 + n * dsn] = v;
+      if (GB_DST(db0 + n * dsn, 1)) reinterpret_cast<C*>(dst)[db0 + n * dsn] = v;
     } else if (KIND == K_C2R) {
       T* d = reinterpret_cast<T*>(dst);
       if (!CONTIG && pvec && has1) {
-        *reinterpret_cast<C*>(d + db0 + n * dsn) = cmk<C>(v.x, -v.y);
+        if (GB_DST(db0 + n * dsn, 2)) *reinterpret_cast<C*>(d + db0 + n * dsn) = cmk<C>(v.x, -v.y);
         return;
       }
-      d[db0 + n * dsn] = v.x;
-      if (has1) d[db1 + n * dsn] = -v.y;
+      if (GB_DST(db0 + n * dsn, 1)) d[db0 + n * dsn] = v.x;
+      if (has1 && GB_DST(db1 + n * dsn, 1)) d[db1 + n * dsn] = -v.y;
     }
   }
 
@@ -592,14 +618,15 @@ struct LineCtx {
       const bool in = (!PRED || valid) && j < h;
       if constexpr (std::is_same<T, float>::value) {
         if (cvec && has1) {  // the pair's two complex values side by side
-          const float4 q = in ? ld4(reinterpret_cast<const float4*>(s + sb0 + j * ssn)) : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 q = (in && GB_SRC(sb0 + j * ssn, 2)) ? ld4(reinterpret_cast<const float4*>(s + sb0 + j * ssn))
+                                                           : make_float4(0.f, 0.f, 0.f, 0.f);
           a[i] = cmk<C>(q.x, q.y);
           b[i] = cmk<C>(q.z, q.w);
           continue;
         }
       }
-      a[i] = in ? ld(s + sb0 + j * ssn) : cmk<C>(T(0), T(0));
-      b[i] = (in && has1) ? ld(s + sb1 + j * ssn) : cmk<C>(T(0), T(0));
+      a[i] = (in && GB_SRC(sb0 + j * ssn, 1)) ? ld(s + sb0 + j * ssn) : cmk<C>(T(0), T(0));
+      b[i] = (in && has1 && GB_SRC(sb1 + j * ssn, 1)) ? ld(s + sb1 + j * ssn) : cmk<C>(T(0), T(0));
     }
 #pragma unroll
     for (int i = 0; i < J; ++i) {
@@ -647,8 +674,8 @@ struct LineCtx {
     for (int k = t; 2 * k <= N; k += tpl) {
       const Pair p = P[sstage(k)];
       const C zk = p.a, zm = p.b;
-      d[db0 + k * dsn] = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
-      if (has1) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
+      if (GB_DST(db0 + k * dsn, 1)) d[db0 + k * dsn] = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
+      if (has1 && GB_DST(db1 + k * dsn, 1)) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
     }
   }
   // The same with the line length NN and its TPL threads known at compile
@@ -670,12 +697,13 @@ struct LineCtx {
       const C x2 = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
       if constexpr (std::is_same<T, float>::value) {
         if (cvec && has1) {  // the pair's two complex outputs side by side
-          *reinterpret_cast<float4*>(d + db0 + k * dsn) = make_float4(x1.x, x1.y, x2.x, x2.y);
+          if (GB_DST(db0 + k * dsn, 2))
+            *reinterpret_cast<float4*>(d + db0 + k * dsn) = make_float4(x1.x, x1.y, x2.x, x2.y);
           continue;
         }
       }
-      d[db0 + k * dsn] = x1;
-      if (has1) d[db1 + k * dsn] = x2;
+      if (GB_DST(db0 + k * dsn, 1)) d[db0 + k * dsn] = x1;
+      if (has1 && GB_DST(db1 + k * dsn, 1)) d[db1 + k * dsn] = x2;
     }
   }
 
@@ -688,8 +716,8 @@ struct LineCtx {
 #pragma unroll 1
     for (int k = t; 2 * k <= N; k += tpl) {
       const C zk = S[sidx(k)], zm = S[sidx(k == 0 ? 0 : N - k)];
-      d[db0 + k * dsn] = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
-      if (has1) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
+      if (GB_DST(db0 + k * dsn, 1)) d[db0 + k * dsn] = cmk<C>((zk.x + zm.x) * h, (zk.y - zm.y) * h);
+      if (has1 && GB_DST(db1 + k * dsn, 1)) d[db1 + k * dsn] = cmk<C>((zk.y + zm.y) * h, (zm.x - zk.x) * h);
     }
   }
 };

@@ -79,7 +79,10 @@ struct PassArgs {
                    // kernel whose tiles arrive by bulk tensor copies
                    // (fft_tma.cu); needs tma_pass_supported()
   int* status;     // device word set to 1 when a bounded wait of the pass
-                   // gave up (null: not recorded)
+                   // gave up, 2 when a check of the bounds-checked build
+                   // caught an access outside an array (null: not recorded)
+  long long src_elems, dst_elems;  // extents of the two arrays in elements of
+                                   // each side's type (bounds-checked build)
   int radix[kMaxStages];
 };
 
@@ -282,6 +285,13 @@ cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous,
 // Enqueue an identity-layout copy of `bytes` bytes (the one-rank transpose).
 cudaError_t launch_copy(const void* src, void* dst, size_t bytes,
                         cudaStream_t stream);
+
+// Every device allocation of the library: cudaMalloc, unless a test armed
+// gbfft_debug_fail_alloc for this one (then cudaErrorMemoryAllocation,
+// nothing allocated).
+cudaError_t dev_malloc(void** p, size_t bytes);
+// ... and every free of one (counts the live allocations)
+cudaError_t dev_free(void* p);
 
 // Record an error message for gbfft_last_error_string(); returns `code`.
 int set_error(int code, const char* msg);

@@ -14,7 +14,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libgbfft.so")
+# GBFFT_LIBRARY selects another build of the library (the bounds-checked
+# lib/debug/libgbfft.so); the default is the product build
+LIB_PATH = os.environ.get("GBFFT_LIBRARY") or os.path.join(HERE, "lib", "libgbfft.so")
 
 OK = 0
 ERR_INVALID = 1
@@ -23,6 +25,7 @@ ERR_CUDA = 3
 ERR_UNSUPPORTED = 4
 ERR_STATE = 5
 ERR_TIMEOUT = 6
+ERR_BOUNDS = 7
 
 PHYSICAL_IN_X = 1
 PHYSICAL_IN_Z = 3
@@ -54,6 +57,10 @@ SIGNATURES = {
     "gbfft_transpose_pack": (_i, [_i, _i, _i, _vp, _i, _i, _i, _i, _ip, _ip, _vp, _sz, _vp]),
     "gbfft_transpose_unpack": (_i, [_i, _i, _i, _vp, _i, _i, _i, _i, _ip, _ip, _sz, _vp, _vp]),
     "gbfft_box_copy": (_i, [_i, _i, _vp, _ip, _ip, _vp, _ip, _ip, _ip, _vp]),
+    "gbfft_debug_fail_alloc": (_i, [ctypes.c_longlong]),
+    "gbfft_debug_live_allocations": (ctypes.c_longlong, []),
+    "gbfft_set_nvtx": (_i, [_i]),
+    "gbfft_debug_bounds_build": (_i, []),
     "gbfft_free": (_i, [_vp]),
     "gbfft_last_error_string": (ctypes.c_char_p, []),
     "gbfft_warning_count": (_i, []),

@@ -32,6 +32,8 @@ extern "C" {
 #define GBFFT_ERR_UNSUPPORTED 4 /* valid request this backend cannot run     */
 #define GBFFT_ERR_STATE 5       /* wrong call order (use before init, ...)   */
 #define GBFFT_ERR_TIMEOUT 6     /* a bounded device wait gave up             */
+#define GBFFT_ERR_BOUNDS 7      /* bounds-checked build: an access outside an
+                                   array was caught (and skipped)            */
 
 /* ---- constants, same values as src/decomp_2d_constants.f90 ----------- */
 #define GBFFT_PHYSICAL_IN_X 1 /* decomp_2d_constants.f90:92 PHYSICAL_IN_X */
@@ -390,6 +392,28 @@ int gbfft_exec_c2r_noalloc(int format, int nx, int ny, int nz, int prec,
  * *timed_out = 1 when the wait gave up (counter_value < need), 0 otherwise.
  * The kernel ends either way; nothing is left waiting on the GPU. */
 int gbfft_selftest_bounded_wait(int counter_value, int need, long long poll_limit, int* timed_out);
+
+/* ---- debugging aids (no counterpart in the reference) ------------------
+ * gbfft_debug_fail_alloc(n): the (n+1)-th device allocation the library
+ * makes from now on (n = 0: the next one) fails as if the device were out of
+ * memory, once; -1 disarms.  Tests drive every allocation of engine, batch
+ * and work-area creation into failure this way and check that each call
+ * returns GBFFT_ERR_ALLOC and frees what it had allocated.
+ * gbfft_set_nvtx(1) names every transform ("fft_r2c", "fft_c2r", "fft_c2c":
+ * the reference's profiler regions, src/fft_common_3d.f90:22,114) and every
+ * axis pass with an NVTX range, for timeline profilers; off by default,
+ * GBFFT_NVTX=1 in the environment turns it on at load.
+ * gbfft_debug_bounds_build() = 1 in a library built with -DGB_DEBUG_BOUNDS
+ * (2decomp-fft_gb300/build.py --variant debug): there every global access of
+ * the axis-pass kernels is checked against its array's extent, and one
+ * outside it is skipped and reported by gbfft_engine_status as
+ * GBFFT_ERR_BOUNDS instead of reaching memory. */
+int gbfft_debug_fail_alloc(long long nth);
+/* Device allocations the library holds right now (engines, batches, work
+ * areas, gbfft_malloc), for leak checks. */
+long long gbfft_debug_live_allocations(void);
+int gbfft_set_nvtx(int enable);
+int gbfft_debug_bounds_build(void);
 
 /* Library version and kernel-launch counter (every kernel this library has
  * enqueued since load), for benchmarks that report launches. */
