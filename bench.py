@@ -50,6 +50,13 @@ WORKLOADS = {
     "r2c_c2r_1024x1024x128_f32_x": (1024, 1024, 128, 1, 4, "gauss_modes"),
     "r2c_c2r_512x256x512_f32_x": (512, 256, 512, 1, 4, "gauss_modes"),
     "r2c_c2r_1024x64x512_f32_x": (1024, 64, 512, 1, 4, "gauss_modes"),
+    # axis lengths off the fast paths: the largest prime one shared-memory tile
+    # takes (a direct-sum stage), a power of two beyond one tile (one radix
+    # stage per kernel through scratch), a prime beyond one tile (a global
+    # direct sum accumulated in double)
+    "r2c_c2r_8191x64x64_f32_x": (8191, 64, 64, 1, 4, "uniform"),
+    "r2c_c2r_65536x32x32_f32_x": (65536, 32, 32, 1, 4, "uniform"),
+    "r2c_c2r_16411x16x16_f64_x": (16411, 16, 16, 1, 8, "uniform"),
 }
 DEFAULT_WORKLOAD = "r2c_c2r_1024x1024x512_f32_x"
 BATCH_WORKLOAD = "batched_64_grids_f32"
@@ -487,11 +494,13 @@ def run_gb300(args):
                         "frac": round(d["gbs"] / peak, 4)}}
     elif dom:
         d = passes[dom]
+        traffic = read_traffic(args.workload + ("" if args.form == "plain" else ":" + args.form), dom)
         roof = {"bound": "hbm", "kernel": "axis pass %s" % dom, "achieved": round(d["gbs"], 1),
                 "peak": peak, "unit": "GB/s", "frac": round(d["gbs"] / peak, 4),
-                "traffic": read_traffic(args.workload + ("" if args.form == "plain" else ":" + args.form), dom),
-                "traffic_source": "committed profile (profiles/dram_traffic.txt: ncu dram bytes of reduced grids "
-                                  "of the same kernel, scaled to a full launch), not measured in this run",
+                "traffic": traffic,
+                "traffic_source": ("committed profile (profiles/dram_traffic.txt: ncu dram bytes of reduced grids "
+                                   "of the same kernel, scaled to a full launch), not measured in this run")
+                if traffic is not None else "no ncu figure committed for this workload and pass",
                 "peak_source": peak_src,
                 "step_frac": round(algo_bytes_step / (ms_max * 1e-3) / 1e9 / peak, 4)}
 
