@@ -15,7 +15,9 @@
 #include <dlfcn.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <algorithm>
 #include <atomic>
+#include <utility>
 #include <cmath>
 #include <cstdlib>
 #include <fstream>
@@ -84,9 +86,26 @@ struct AxisPlan {
   int fast_e = 16;    // points per thread of the power-of-two kernel
   bool big = false;   // lines do not fit one shared-memory tile: the
                       // multi-kernel long-axis path (fft_long.cu)
+  bool blue = false;  // a prime factor above kBluePrime: the chirp-z path
+                      // of fft_long.cu (implies big)
   void* d_tw = nullptr;   // exp(-2 pi i m / n), m = 0..n-1
   void* d_twf = nullptr;  // stage-major table of the power-of-two kernel
+  void* d_chirp = nullptr;  // chirp-z tables (bt points at them)
+  void* d_filt = nullptr;
+  void* d_twm = nullptr;
+  BlueTables bt{};
 };
+
+// Largest prime factor of an axis's length, from its radix stages (the
+// power-of-two radices 16/8/4 count as 2).
+int largest_prime(const AxisPlan& p) {
+  int q = 1;
+  for (int i = 0; i < p.nst; ++i) {
+    const int r = p.radix[i];
+    q = std::max(q, (r == 16 || r == 8 || r == 4) ? 2 : r);
+  }
+  return q;
+}
 
 // Split n into radix stages: 16s, then one 8/4/2 for the rest of the powers
 // of two, then 7s, 5s, 3s, then any other prime as a generic stage.  Largest
@@ -210,10 +229,83 @@ std::vector<int> plan_radices(const AxisPlan& p) {
   return radices;
 }
 
+// Forward DFT of a (power-of-two length) in place, iterative radix 2, in
+// double with roots evaluated in long double: the chirp-z filter.
+void host_fft_pow2(std::vector<double>& a) {
+  const size_t m = a.size() / 2;
+  for (size_t i = 1, j = 0; i < m; ++i) {
+    size_t bit = m >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) {
+      std::swap(a[2 * i], a[2 * j]);
+      std::swap(a[2 * i + 1], a[2 * j + 1]);
+    }
+  }
+  const std::vector<double> root = twiddles((int)m);  // exp(-2 pi i k / m)
+  for (size_t len = 2; len <= m; len <<= 1) {
+    const size_t half = len / 2, step = m / len;
+    for (size_t i = 0; i < m; i += len)
+      for (size_t k = 0; k < half; ++k) {
+        const double wr = root[2 * k * step], wi = root[2 * k * step + 1];
+        double* u = &a[2 * (i + k)];
+        double* v = &a[2 * (i + k + half)];
+        const double tr = v[0] * wr - v[1] * wi, ti = v[0] * wi + v[1] * wr;
+        v[0] = u[0] - tr;
+        v[1] = u[1] - ti;
+        u[0] += tr;
+        u[1] += ti;
+      }
+  }
+}
+
+// Chirp-z tables of an axis: w_j = exp(-i pi j^2 / n) (j^2 reduced mod 2n
+// exactly), FFT_m(b) / m with b_j = b_(m-j) = conj w_j, the m roots, and
+// the radix plan of m (16s, then one 8/4/2).
+int upload_blue(AxisPlan& p, int prec) {
+  const int n = p.n;
+  long long m = 1;
+  while (m < 2LL * n - 1) m <<= 1;
+  if (m > (1LL << 27)) return fail(GBFFT_ERR_UNSUPPORTED, "axis too long for the chirp-z path");
+  const long double pi = 3.141592653589793238462643383279502884L;
+  std::vector<double> w(2 * (size_t)n), b(2 * (size_t)m, 0.0);
+  for (long long j = 0; j < n; ++j) {
+    const unsigned long long e = ((unsigned long long)j * (unsigned long long)j) % (2ULL * (unsigned long long)n);
+    const long double a = pi * (long double)e / (long double)n;
+    const double c = (double)cosl(a), sn = (double)sinl(a);
+    w[2 * j] = c;
+    w[2 * j + 1] = -sn;
+    b[2 * j] = c;
+    b[2 * j + 1] = sn;
+    if (j > 0) {
+      b[2 * (m - j)] = c;
+      b[2 * (m - j) + 1] = sn;
+    }
+  }
+  host_fft_pow2(b);
+  for (double& v : b) v /= (double)m;
+  int rc = upload_table(&p.d_chirp, w, prec);
+  if (rc == GBFFT_OK) rc = upload_table(&p.d_filt, b, prec);
+  if (rc == GBFFT_OK) rc = upload_table(&p.d_twm, twiddles((int)m), prec);
+  if (rc != GBFFT_OK) return rc;
+  BlueTables& t = p.bt;
+  t.m = (int)m;
+  t.nst = 0;
+  int lg = 0;
+  while ((1LL << lg) < m) ++lg;
+  for (; lg >= 4; lg -= 4) t.radix[t.nst++] = 16;
+  if (lg > 0) t.radix[t.nst++] = 1 << lg;
+  t.chirp = p.d_chirp;
+  t.filt = p.d_filt;
+  t.twm = p.d_twm;
+  return GBFFT_OK;
+}
+
 int upload_twiddles(AxisPlan& p, int prec) {
   int rc = upload_table(&p.d_tw, twiddles(p.n), prec);
   const std::vector<int> radices = plan_radices(p);
   if (rc == GBFFT_OK && !radices.empty()) rc = upload_table(&p.d_twf, stage_twiddles(radices), prec);
+  if (rc == GBFFT_OK && p.blue) rc = upload_blue(p, prec);
   return rc;
 }
 
@@ -363,10 +455,10 @@ void drop_profile(gbfft_engine_t e) {
 void release(gbfft_engine_t e) {
   drop_profile(e);
   for (auto& a : e->ax) {
-    if (a.d_tw) dev_free(a.d_tw);
-    if (a.d_twf) dev_free(a.d_twf);
-    a.d_tw = nullptr;
-    a.d_twf = nullptr;
+    for (void** q : {&a.d_tw, &a.d_twf, &a.d_chirp, &a.d_filt, &a.d_twm}) {
+      if (*q) dev_free(*q);
+      *q = nullptr;
+    }
   }
   if (e->work) dev_free(e->work);
   e->work = nullptr;
@@ -500,6 +592,7 @@ int gen_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int fo
 
 void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int kind, int forced_L,
                bool split = false, int csize = 0, int csync = 0) {
+  a.blue = p.blue ? &p.bt : nullptr;
   if (split && split_length(p.n)) {
     a.n = p.n;
     a.nst = 0;
@@ -877,6 +970,10 @@ int engine_init_host(gbfft_engine_s* e, int format, int nx, int ny, int nz, int 
     if (!factorize(lens[d], e->ax[d], why)) return fail(GBFFT_ERR_UNSUPPORTED, why);
     // lines longer than one shared-memory tile take the long-axis path
     e->ax[d].big = lens[d] > kMaxN || pass_smem_bytes(prec, lens[d], 1) > 200 * 1024;
+    // a large prime factor: the chirp-z transform (O(n log n)) instead of a
+    // direct-sum stage (O(p) a point)
+    e->ax[d].blue = largest_prime(e->ax[d]) > kBluePrime;
+    if (e->ax[d].blue) e->ax[d].big = true;
     e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
     if (gen_length(lens[d])) e->ax[d].fast_e = gen_points(lens[d]);
     if (fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
@@ -1144,7 +1241,12 @@ int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace, const i
   // scratch of the long-axis path: two copies of the largest pass's lines,
   // at most the whole grid in complex values (any engine may run c2c)
   if (e->ax[0].big || e->ax[1].big || e->ax[2].big) {
-    e->long_scratch_bytes = 2 * (size_t)nx * ny * nz * cbytes(e);
+    // the chirp-z path keeps lines of m points: at most grid / n lines of a pass
+    const size_t grid = (size_t)nx * ny * nz;
+    size_t pts = grid;
+    for (const AxisPlan& a : e->ax)
+      if (a.blue) pts = std::max(pts, grid / (size_t)a.n * (size_t)a.bt.m);
+    e->long_scratch_bytes = 2 * pts * cbytes(e);
     cudaError_t err = dev_malloc(&e->long_scratch, e->long_scratch_bytes);
     if (err != cudaSuccess) {
       e->long_scratch = nullptr;

@@ -27,6 +27,16 @@
 //    coalesced.
 // Each stage reads and writes the whole array, so a long axis costs about
 // (stages + 2) sweeps instead of one.
+//
+// Lengths with a prime factor above kBluePrime (in or beyond one tile) run
+// the chirp-z transform instead of a direct sum (Bluestein's algorithm):
+// with w_j = exp(-i pi j^2 / n), jk = (j^2 + k^2 - (k - j)^2) / 2 gives
+//   X_k = w_k sum_j (x_j w_j) conj(w_(k-j)),
+// a circular convolution of length m (a power of two >= 2n - 1) of the
+// zero-padded a_j = x_j w_j with b (conj w_j at j and m - j).  It runs as
+// chirp-in (a, n -> m points), an m-point FFT, a pointwise product with
+// FFT_m(b) / m conjugated, a second m-point FFT, and chirp-out
+// (X_k = w_k conj F_k, m -> n points): O(n log n) instead of O(n p).
 #include <algorithm>
 #include <atomic>
 
@@ -252,6 +262,77 @@ __global__ void __launch_bounds__(kThreads) unpack_kernel(const __grid_constant_
   }
 }
 
+
+// ---- chirp-z path
+struct ChirpArgs {
+  Side in, out;
+  const void* chirp;  // w_j, j < n
+  const void* filt;   // FFT_m(b) / m
+  long long lines, nu;
+  int n, m;
+  int conj_in, conj_out;
+};
+
+// a_j = x_j w_j (j < n), 0 (n <= j < m): the pass's (or a packed) line in,
+// an m-point scratch line out
+template <typename T, bool UFAST>
+__global__ void __launch_bounds__(kThreads) chirp_in_kernel(const __grid_constant__ ChirpArgs a) {
+  using C = Cx<T>;
+  const C* in = static_cast<const C*>(a.in.p);
+  C* out = static_cast<C*>(a.out.p);
+  const C* w = static_cast<const C*>(a.chirp);
+  const long long total = a.lines * a.m;
+  for (long long idx = (long long)blockIdx.x * kThreads + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * kThreads) {
+    const long long l = UFAST ? idx % a.lines : idx / a.m, j = UFAST ? idx / a.lines : idx % a.m;
+    C y{T(0), T(0)};
+    if (j < a.n) {
+      C x = in[line_off(a.in, l, a.nu) + j * a.in.s_n];
+      if (a.conj_in) x.y = -x.y;
+      y = cmul(x, w[j]);
+    }
+    out[line_off(a.out, l, a.nu) + j * a.out.s_n] = y;
+  }
+}
+
+// in place: A_k <- conj(A_k FFT_m(b)_k / m), so that the next forward FFT
+// gives the conjugate of the convolution
+template <typename T, bool UFAST>
+__global__ void __launch_bounds__(kThreads) chirp_filter_kernel(const __grid_constant__ ChirpArgs a) {
+  using C = Cx<T>;
+  C* buf = static_cast<C*>(a.out.p);
+  const C* f = static_cast<const C*>(a.filt);
+  const long long total = a.lines * a.m;
+  for (long long idx = (long long)blockIdx.x * kThreads + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * kThreads) {
+    const long long l = UFAST ? idx % a.lines : idx / a.m, k = UFAST ? idx / a.lines : idx % a.m;
+    const long long o = line_off(a.out, l, a.nu) + k * a.out.s_n;
+    C p = cmul(buf[o], f[k]);
+    p.y = -p.y;
+    buf[o] = p;
+  }
+}
+
+// X_k = w_k conj(F_k), k < n: an m-point scratch line in, the pass's (or a
+// scratch) line out
+template <typename T, bool UFAST>
+__global__ void __launch_bounds__(kThreads) chirp_out_kernel(const __grid_constant__ ChirpArgs a) {
+  using C = Cx<T>;
+  const C* in = static_cast<const C*>(a.in.p);
+  C* out = static_cast<C*>(a.out.p);
+  const C* w = static_cast<const C*>(a.chirp);
+  const long long total = a.lines * a.n;
+  for (long long idx = (long long)blockIdx.x * kThreads + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * kThreads) {
+    const long long l = UFAST ? idx % a.lines : idx / a.n, k = UFAST ? idx / a.lines : idx % a.n;
+    C f = in[line_off(a.in, l, a.nu) + k * a.in.s_n];
+    f.y = -f.y;
+    C x = cmul(w[k], f);
+    if (a.conj_out) x.y = -x.y;
+    out[line_off(a.out, l, a.nu) + k * a.out.s_n] = x;
+  }
+}
+
 int sm_count() {
   static std::atomic<int> cached{0};
   int v = cached.load();
@@ -403,16 +484,153 @@ cudaError_t run(int kind, const PassArgs& a, void* scratch, size_t scratch_bytes
   return cudaGetLastError();
 }
 
+
+// The chirp-z pass: pack / merge (real passes), chirp-in, m-point FFT,
+// filter, m-point FFT, chirp-out, split / unpack (real passes).  Scratch:
+// two buffers of `lines` m-point lines; the packed n-point lines sit in
+// buffer 1 until chirp-in has read them.
+template <typename T, bool UFAST>
+cudaError_t run_blue(int kind, const PassArgs& a, void* scratch, size_t scratch_bytes, cudaStream_t st) {
+  using C = Cx<T>;
+  const BlueTables& b = *a.blue;
+  const int n = a.n, m = b.m;
+  const bool contig = !UFAST;
+  const long long nu = a.nlines, lines = a.nlines * (contig ? 1 : (long long)a.nv);
+  const size_t need = (size_t)lines * m * sizeof(C);
+  if (2 * need > scratch_bytes) return cudaErrorInvalidValue;
+  C* sb[2] = {static_cast<C*>(scratch), reinterpret_cast<C*>(static_cast<char*>(scratch) + need)};
+  auto scratch_side = [&](int i, int len) {
+    Side s;
+    s.p = sb[i];
+    if (UFAST) {
+      s.s_u = 1;
+      s.s_v = nu;
+      s.s_n = lines;
+    } else {
+      s.s_u = len;
+      s.s_v = (long long)len * nu;
+      s.s_n = 1;
+    }
+    return s;
+  };
+  auto side = [&](const void* p, long long s_n, long long s_l) {
+    Side s;
+    s.p = const_cast<void*>(p);
+    s.s_n = s_n;
+    s.s_u = contig ? s_l : 1;
+    s.s_v = contig ? 0 : s_l;
+    return s;
+  };
+  const Side src = side(a.src, a.s_src_n, a.s_src_l), dst = side(a.dst, a.s_dst_n, a.s_dst_l);
+  RealArgs ra;
+  ra.lines = lines;
+  ra.nu = nu;
+  ra.real_u = a.real_lines;
+  ra.n = n;
+  cudaError_t err;
+  ChirpArgs ca;
+  ca.chirp = b.chirp;
+  ca.filt = b.filt;
+  ca.lines = lines;
+  ca.nu = nu;
+  ca.n = n;
+  ca.m = m;
+  ca.in = src;
+  ca.conj_in = a.inverse;
+  ca.conj_out = 0;
+  if (kind == K_R2C || kind == K_C2R) {
+    ra.s = scratch_side(1, n);
+    if (kind == K_R2C) {
+      ra.re = src;
+      pack_kernel<T, UFAST><<<grid_for(lines * (long long)n), kThreads, 0, st>>>(ra);
+    } else {
+      ra.cx = src;
+      merge_kernel<T, UFAST><<<grid_for(lines * (long long)n), kThreads, 0, st>>>(ra);
+    }
+    add_launches(1);
+    ca.in = scratch_side(1, n);
+    ca.conj_in = 0;
+  }
+  ca.out = scratch_side(0, m);
+  chirp_in_kernel<T, UFAST><<<grid_for(lines * (long long)m), kThreads, 0, st>>>(ca);
+  add_launches(1);
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  int cur = 0;
+  for (int round = 0; round < 2; ++round) {
+    int ns = 1;
+    for (int s = 0; s < b.nst; ++s) {
+      const int R = b.radix[s];
+      StageArgs sa;
+      sa.in = scratch_side(cur, m);
+      sa.out = scratch_side(1 - cur, m);
+      sa.tw = b.twm;
+      sa.lines = lines;
+      sa.nu = nu;
+      sa.m = m / R;
+      sa.n = m;
+      sa.R = R;
+      sa.NS = ns;
+      sa.conj_in = 0;
+      sa.conj_out = 0;
+      if ((err = launch_stage<T, UFAST>(sa, st)) != cudaSuccess) return err;
+      cur = 1 - cur;
+      ns *= R;
+    }
+    if (round == 0) {
+      ca.out = scratch_side(cur, m);
+      chirp_filter_kernel<T, UFAST><<<grid_for(lines * (long long)m), kThreads, 0, st>>>(ca);
+      add_launches(1);
+      if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    }
+  }
+  ca.in = scratch_side(cur, m);
+  if (kind == K_C2C) {
+    ca.out = dst;
+    ca.conj_out = a.inverse;
+  } else {
+    ca.out = scratch_side(1 - cur, n);
+    ca.conj_out = 0;
+  }
+  chirp_out_kernel<T, UFAST><<<grid_for(lines * (long long)n), kThreads, 0, st>>>(ca);
+  add_launches(1);
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  if (kind == K_R2C) {
+    ra.s = scratch_side(1 - cur, n);
+    ra.cx = dst;
+    split_kernel<T, UFAST><<<grid_for(lines * (long long)(n / 2 + 1)), kThreads, 0, st>>>(ra);
+    add_launches(1);
+  } else if (kind == K_C2R) {
+    ra.s = scratch_side(1 - cur, n);
+    ra.re = dst;
+    unpack_kernel<T, UFAST><<<grid_for(lines * (long long)n), kThreads, 0, st>>>(ra);
+    add_launches(1);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace lng
 
 size_t long_pass_scratch_bytes(int prec_bytes, bool contiguous, const PassArgs& a) {
   const long long lines = a.nlines * (contiguous ? 1 : (long long)a.nv);
-  return 2 * (size_t)lines * (size_t)a.n * 2 * (size_t)prec_bytes;
+  const long long len = a.blue ? a.blue->m : a.n;
+  return 2 * (size_t)lines * (size_t)len * 2 * (size_t)prec_bytes;
 }
 
 cudaError_t launch_long_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a, void* scratch,
                              size_t scratch_bytes, cudaStream_t stream) {
-  if (a.row_w != 0 || a.nst < 1 || !a.tw || !scratch) return cudaErrorInvalidValue;
+  if (a.row_w != 0 || !scratch) return cudaErrorInvalidValue;
+  if (a.blue) {
+    const BlueTables& b = *a.blue;
+    if (b.m < 2 * a.n - 1 || b.nst < 1 || !b.chirp || !b.filt || !b.twm) return cudaErrorInvalidValue;
+    if (prec_bytes == 4)
+      return contiguous ? lng::run_blue<float, false>(kind, a, scratch, scratch_bytes, stream)
+                        : lng::run_blue<float, true>(kind, a, scratch, scratch_bytes, stream);
+    if (prec_bytes == 8)
+      return contiguous ? lng::run_blue<double, false>(kind, a, scratch, scratch_bytes, stream)
+                        : lng::run_blue<double, true>(kind, a, scratch, scratch_bytes, stream);
+    return cudaErrorInvalidValue;
+  }
+  if (a.nst < 1 || !a.tw) return cudaErrorInvalidValue;
   if (kind == K_C2C && a.n < 1) return cudaErrorInvalidValue;
   if (prec_bytes == 4)
     return contiguous ? lng::run<float, false>(kind, a, scratch, scratch_bytes, stream)

@@ -41,6 +41,24 @@ __host__ __device__ constexpr bool radix_is_special(int r) {
 // For K_R2C / K_C2R two neighbouring real lines (2c, 2c+1 along l or u) are
 // carried by one complex line c.  All strides are in elements of the
 // array's own type (real elements for the real side of r2c/c2r).
+// Chirp-z (Bluestein) tables of one axis whose length has a large prime
+// factor: the length-n transform is a circular convolution of length m (a
+// power of two >= 2n - 1) between the input times a chirp and the
+// conjugate chirp, done as two forward m-point FFTs.  Device pointers; the
+// struct itself lives on the host, in the engine's axis plan.
+struct BlueTables {
+  int m;                    // convolution length
+  int nst;                  // radix stages of the m-point FFTs
+  int radix[kMaxStages];
+  const void* chirp;        // w_j = exp(-i pi j^2 / n), j < n
+  const void* filt;         // FFT_m of b (b_j = conj w_j at j and m - j, 0 between), divided by m
+  const void* twm;          // exp(-2 pi i k / m), k < m
+};
+
+// Axes whose largest prime factor exceeds this run the chirp-z path: a
+// direct-sum stage costs that many multiply-adds a point.
+constexpr int kBluePrime = 256;
+
 struct PassArgs {
   const void* src;
   void* dst;
@@ -83,6 +101,8 @@ struct PassArgs {
                    // caught an access outside an array (null: not recorded)
   long long src_elems, dst_elems;  // extents of the two arrays in elements of
                                    // each side's type (bounds-checked build)
+  const BlueTables* blue;  // host-side tables of the chirp-z path (fft_long.cu),
+                           // null unless the axis runs it; never read on the device
   int radix[kMaxStages];
 };
 
@@ -270,10 +290,12 @@ bool tma_pass_supported(int prec_bytes, int kind, bool contiguous, const PassArg
 cudaError_t launch_tma_pass(const PassArgs& a, cudaStream_t stream);
 long long tma_launch_counter();
 
-// Axis passes whose lines do not fit one shared-memory tile (fft_long.cu):
-// one kernel per radix stage through `scratch`, which must hold two copies
-// of the pass's lines (long_pass_scratch_bytes).  Lines are per row (row_w
-// = 0); a.nst / a.radix are the axis's stages, a.tw its n-root table.
+// Axis passes whose lines do not fit one shared-memory tile, or whose
+// length has a prime factor above kBluePrime (fft_long.cu): one kernel per
+// radix stage through `scratch`, which must hold two copies of the pass's
+// lines -- of m points each on the chirp-z path (long_pass_scratch_bytes).
+// Lines are per row (row_w = 0); a.nst / a.radix are the axis's stages,
+// a.tw its n-root table, a.blue the chirp-z tables when set.
 size_t long_pass_scratch_bytes(int prec_bytes, bool contiguous, const PassArgs& a);
 cudaError_t launch_long_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a, void* scratch,
                              size_t scratch_bytes, cudaStream_t stream);

@@ -1,8 +1,9 @@
 """GPU: axes longer than one shared-memory tile -- more than 8192 points, or
 FP64 lines whose two tile buffers do not fit -- run stage by stage through
 global memory (the long-axis path), for any length: powers of two, mixed
-radices, large primes as one direct-sum stage (the reference's SPCFFT takes
-any N: src/glassman.f90:29-67).  Every case through the C ABI against the
+radices and primes up to 256 as direct-sum stages, larger primes as the
+chirp-z transform (the reference's SPCFFT takes any N:
+src/glassman.f90:29-67).  Every case through the C ABI against the
 FP64 oracle and against pocketfft (numpy) in FP64.  Tolerances as the parity
 tests, rel-L2 <= 1e-12 in double, <= 2e-6 in single, against pocketfft; and
 against the oracle the same plus the oracle's own distance from pocketfft:
@@ -57,7 +58,7 @@ def _engine(fmt, shape, prec, skip=None):
 
 
 # one long axis each: 2^14; 2^4 5^4 = 10000 (mixed radix); 8209 (prime:
-# one direct-sum stage); 73 * 137 = 10001 (two generic prime stages)
+# the chirp-z path); 73 * 137 = 10001 (two generic prime stages)
 C2C_CASES = [((16384, 3, 2), "s"), ((16384, 2, 2), "d"), ((5, 10000, 3), "s"), ((4, 3, 9000), "d"),
              ((8209, 2, 2), "s"), ((3, 10001, 2), "s"), ((2, 2, 8209), "d")]
 
