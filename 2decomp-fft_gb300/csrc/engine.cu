@@ -90,6 +90,8 @@ struct AxisPlan {
                       // of fft_long.cu (implies big)
   void* d_tw = nullptr;   // exp(-2 pi i m / n), m = 0..n-1
   void* d_twf = nullptr;  // stage-major table of the power-of-two kernel
+  void* d_twf16 = nullptr;  // the same for 16 points a thread, when the axis
+                            // runs 4 or 8 (the batch kernel's plan)
   void* d_chirp = nullptr;  // chirp-z tables (bt points at them)
   void* d_filt = nullptr;
   void* d_twm = nullptr;
@@ -301,11 +303,21 @@ int upload_blue(AxisPlan& p, int prec) {
   return GBFFT_OK;
 }
 
+// The batch kernel runs 16 points a thread on power-of-two lines: an axis
+// on 4 or 8 also keeps that plan's stage-major table.
+int upload_batch_table(AxisPlan& p, int prec) {
+  if (!fast_length(p.n) || (p.fast_e != 4 && p.fast_e != 8) || p.d_twf16) return GBFFT_OK;
+  AxisPlan q = p;
+  q.fast_e = 16;
+  return upload_table(&p.d_twf16, stage_twiddles(plan_radices(q)), prec);
+}
+
 int upload_twiddles(AxisPlan& p, int prec) {
   int rc = upload_table(&p.d_tw, twiddles(p.n), prec);
   const std::vector<int> radices = plan_radices(p);
   if (rc == GBFFT_OK && !radices.empty()) rc = upload_table(&p.d_twf, stage_twiddles(radices), prec);
   if (rc == GBFFT_OK && p.blue) rc = upload_blue(p, prec);
+  if (rc == GBFFT_OK) rc = upload_batch_table(p, prec);
   return rc;
 }
 
@@ -455,7 +467,7 @@ void drop_profile(gbfft_engine_t e) {
 void release(gbfft_engine_t e) {
   drop_profile(e);
   for (auto& a : e->ax) {
-    for (void** q : {&a.d_tw, &a.d_twf, &a.d_chirp, &a.d_filt, &a.d_twm}) {
+    for (void** q : {&a.d_tw, &a.d_twf, &a.d_twf16, &a.d_chirp, &a.d_filt, &a.d_twm}) {
       if (*q) dev_free(*q);
       *q = nullptr;
     }
@@ -521,7 +533,8 @@ int lines_per_cta(const AxisPlan& p, int prec, bool contiguous, long long nlines
 
 // Lines per CTA for the power-of-two kernel (n / fast_points(n) threads per
 // line).
-int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int forced_L, int e) {
+int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int forced_L, int e,
+                       long long nv = 1) {
   const int tpl = n / e;
   if (forced_L > 0) return forced_L;
   const int maxt = fast_max_threads(e, prec);
@@ -540,6 +553,10 @@ int fast_lines_per_cta(int n, int prec, bool contiguous, long long nlines, int f
   while (L > 1 && L * tpl > maxt) L /= 2;
   while (L > 1 && (size_t)fast_smem_entries(n, L) * 2 * prec > 100 * 1024) L /= 2;
   if (L < 1) L = 1;
+  // small grids: fewer lines a CTA until there are two CTAs per SM (strided
+  // tiles keep at least 64-byte row segments)
+  const int min_keep = contiguous ? 1 : (int)(64 / (2 * prec));
+  while (L > min_keep && ((nlines + L - 1) / L) * nv < 2LL * kSmsDefault) L /= 2;
   if (L > 1 && nlines < L) {
     int l2 = 1;
     while (l2 < nlines) l2 *= 2;
@@ -635,7 +652,7 @@ void fill_plan(PassArgs& a, const AxisPlan& p, int prec, bool contiguous, int ki
     a.fast = 1;
     const int fe = p.fast_e;  // only axis 0 runs contiguous lines
     a.tpl = p.n / fe;
-    a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L, fe);
+    a.L = fast_lines_per_cta(p.n, prec, contiguous, a.nlines, forced_L, fe, contiguous ? 1 : a.nv);
     a.first_fused = 1;
     a.last_fused = kind != K_R2C;
     a.csize = csize > 1 ? csize : 0;
@@ -975,8 +992,16 @@ int engine_init_host(gbfft_engine_s* e, int format, int nx, int ny, int nz, int 
     e->ax[d].blue = largest_prime(e->ax[d]) > kBluePrime;
     if (e->ax[d].blue) e->ax[d].big = true;
     e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
+    if (fast_length(lens[d]) && lens[d] <= 256) {
+      // short lines of a small grid: fewer points a thread until the pass
+      // has about 16 warps per SM (lines of a full-grid pass: grid / n)
+      const double lines = (double)nx * ny * nz / lens[d];
+      int pe = 16;
+      while (pe > 4 && fast_e_ok(lens[d], pe / 2) && lines * (lens[d] / pe) < 512.0 * kSmsDefault) pe /= 2;
+      e->ax[d].fast_e = pe;
+    }
     if (gen_length(lens[d])) e->ax[d].fast_e = gen_points(lens[d]);
-    if (fast_has_alt(lens[d]) && tune.e[d] > 0) e->ax[d].fast_e = tune.e[d];
+    if (fast_has_alt(lens[d]) && tune.e[d] > 0 && fast_e_ok(lens[d], tune.e[d])) e->ax[d].fast_e = tune.e[d];
     if (gen_length(lens[d]) && (tune.e[d] == gen_points(lens[d]) || tune.e[d] == 2))
       e->ax[d].fast_e = tune.e[d];
     if (form == GBFFT_FORM_SPLIT && split_length(lens[d])) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
@@ -1081,7 +1106,17 @@ int gbfft::engine_passes(gbfft_engine_s* e, int which, const void* in, void* out
   std::vector<Pass> ps =
       which == 0 ? r2c_passes(e, in, out) : c2r_passes(e, const_cast<void*>(in), out);
   if ((int)ps.size() > max_passes) return fail(GBFFT_ERR_INVALID, "too many passes");
-  for (size_t i = 0; i < ps.size(); ++i) out_passes[i] = PassInfo{ps[i].a, ps[i].kind, ps[i].contiguous};
+  for (size_t i = 0; i < ps.size(); ++i) {
+    PassInfo q{ps[i].a, ps[i].kind, ps[i].contiguous};
+    // the batch kernel's power-of-two plan is 16 points a thread
+    if (q.a.fast == 1)
+      for (const AxisPlan& ax : e->ax)
+        if (q.a.tw == ax.d_twf && ax.d_twf16) {
+          q.a.tw = ax.d_twf16;
+          q.a.tpl = q.a.n / fast_points(q.a.n, q.contiguous);
+        }
+    out_passes[i] = q;
+  }
   *n = (int)ps.size();
   return GBFFT_OK;
 }
@@ -1516,7 +1551,9 @@ int gbfft_engine_set_plan(gbfft_engine_t e, int axis, int points) {
       return fail(GBFFT_ERR_INVALID, "points per thread must be the balanced plan's or 2 (two-stage plan)");
   } else {
     if (!fast_has_alt(p.n)) return fail(GBFFT_ERR_UNSUPPORTED, "this axis length has one plan");
-    if (points != 16 && points != 32) return fail(GBFFT_ERR_INVALID, "points per thread must be 16 or 32");
+    if (!fast_e_ok(p.n, points))
+      return fail(GBFFT_ERR_INVALID, "points per thread must be 32 or 16 (512 and 1024 points) or 16, 8, 4 "
+                                     "(8: at most 256 points, 4: at most 128)");
   }
   if (p.fast_e == points) return GBFFT_OK;
   void* old = p.d_twf;
@@ -1531,6 +1568,7 @@ int gbfft_engine_set_plan(gbfft_engine_t e, int axis, int points) {
   }
   cudaDeviceSynchronize();  // no pass still reads the old table
   if (old) dev_free(old);
+  if ((rc = upload_batch_table(p, e->prec)) != GBFFT_OK) return rc;
   for (int k = 0; k < GBFFT_PASS_KINDS; ++k) e->tile_L[k] = 0;  // tiles were sized for the old plan
   return GBFFT_OK;
 }

@@ -253,6 +253,11 @@ cudaError_t launch_n(const PassArgs& a, cudaStream_t stream) {
     if (a.tpl == N / 16) return launch_ne<T, KIND, CONTIG, N, 16>(a, stream);
     return launch_ne<T, KIND, CONTIG, N, 32>(a, stream);
   } else {
+    // short lines: 4 or 8 points a thread when the engine chose them
+    if constexpr (N <= 128)
+      if (a.tpl == N / 4) return launch_ne<T, KIND, CONTIG, N, 4>(a, stream);
+    if constexpr (N <= 256)
+      if (a.tpl == N / 8) return launch_ne<T, KIND, CONTIG, N, 8>(a, stream);
     return launch_ne<T, KIND, CONTIG, N, fast_points(N, CONTIG)>(a, stream);
   }
 }

@@ -16,6 +16,7 @@ constexpr int kMaxE = 16;         // complex values a thread holds in one stage
 constexpr int kMaxThreads = 512;  // threads in one CTA of an axis pass
 constexpr int kMaxN = 8192;       // longest axis a single-tile pass supports
 constexpr int kMaxGridY = 65535;  // planes (grid.y) of one strided launch
+constexpr int kSmsDefault = 152;  // SMs of a GB300: the occupancy targets of small grids
 
 // What one axis pass does to each line.
 enum Kind : int {
@@ -113,19 +114,29 @@ __host__ __device__ constexpr bool fast_length(int n) {
 }
 // Radix plan of the power-of-two kernel, for E points per thread.  E = 32
 // (strided y/z lines of length 512 or 1024): two stages, 32 x (n/32), one
-// exchange.  E = 16 (everything else): radix 16 stages, then one stage of
-// the remaining factor 2, 4 or 8.
+// exchange.  E = 16 (the default), 8 or 4: radix-E stages, then one stage
+// of the remaining factor.  E = 8 (lines of at most 256 points) and E = 4
+// (at most 128) give short lines more threads, for grids too small to
+// fill the GPU at 16 points a thread.
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 __host__ __device__ constexpr int fast_points(int n, bool contiguous) {
   return (!contiguous && (n == 512 || n == 1024)) ? 32 : 16;
 }
-// Lengths whose strided passes also have the other plan (16 points a thread).
-__host__ __device__ constexpr bool fast_has_alt(int n) { return n == 512 || n == 1024; }
+// Points per thread the power-of-two kernel offers for length n.
+__host__ __device__ constexpr bool fast_e_ok(int n, int e) {
+  return n >= 16 && n <= 4096 && (n & (n - 1)) == 0 &&
+         (e == 16 || (e == 32 && (n == 512 || n == 1024)) || (e == 8 && n <= 256) || (e == 4 && n <= 128));
+}
+// Lengths with more than one power-of-two plan.
+__host__ __device__ constexpr bool fast_has_alt(int n) {
+  return n == 512 || n == 1024 || (n >= 16 && n <= 256 && (n & (n - 1)) == 0);
+}
 __host__ __device__ constexpr int fast_nst(int n, int e) {
-  return e == 32 ? 2 : ilog2c(n) / 4 + (ilog2c(n) % 4 ? 1 : 0);
+  return e == 32 ? 2 : ilog2c(n) / ilog2c(e) + (ilog2c(n) % ilog2c(e) ? 1 : 0);
 }
 __host__ __device__ constexpr int fast_radix(int n, int e, int s) {
-  return e == 32 ? (s == 0 ? 32 : n / 32) : (s < ilog2c(n) / 4 ? 16 : (1 << (ilog2c(n) % 4)));
+  return e == 32 ? (s == 0 ? 32 : n / 32)
+                 : (s < ilog2c(n) / ilog2c(e) ? e : (1 << (ilog2c(n) % ilog2c(e))));
 }
 // Thread limits of the power-of-two kernel, launched with one CTA per SM
 // guaranteed: 16 points a thread at most 64 registers (1024 threads, FP32),

@@ -4,7 +4,8 @@ For each grid shape it measures, on the GPU at hand, the choices an engine
 can make and writes the fastest into the tuning cache that engines read at
 creation (tune_cache.txt beside this file, or $GBFFT_TUNE_CACHE):
 
-  * the radix plan of axes of 512 or 1024 points: 16 points per thread
+  * the radix plan of power-of-two axes: 16 or 8 or 4 points a thread on lines
+    of at most 256 points (8) or 128 (4); of axes of 512 or 1024 points: 16 points per thread
     (radix 16 stages) or 32 (two radix-32 stages); of axes of 243, 270,
     360, 384, 400 points: the balanced plan or the two-stage one (2)
                                                                -> e_x, e_y, e_z
@@ -90,7 +91,16 @@ def tune_shape(prec, fmt, nx, ny, nz, log=print):
     opts = {}
     balanced = {243: 9, 270: 30, 360: 30, 384: 24, 400: 20}  # points of the balanced plans
     for axis, n in ((0, nx), (1, ny), (2, nz)):
-        opts[axis] = [16, 32] if n in (512, 1024) else ([balanced[n], 2] if n in balanced else [None])
+        if n in (512, 1024):
+            opts[axis] = [16, 32]
+        elif n in balanced:
+            opts[axis] = [balanced[n], 2]
+        elif n in (16, 32, 64, 128):
+            opts[axis] = [16, 8, 4]  # short lines: more threads on small grids
+        elif n == 256:
+            opts[axis] = [16, 8]
+        else:
+            opts[axis] = [None]
     eng.set_fusion(False)
 
     def apply(ex, ey, ez, layout, tma):

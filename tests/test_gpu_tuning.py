@@ -156,3 +156,69 @@ def test_cache_line_is_applied(tmp_path):
         other.close()
     finally:
         gbfft.set_tune_cache(None)
+
+
+# short power-of-two lines: 16, 8 or 4 points a thread (8: at most 256
+# points, 4: at most 128), on every axis, both precisions, r2c / c2r / c2c
+SHORT = [(n, pe) for n in (16, 32, 64, 128, 256) for pe in (16, 8, 4) if pe == 16 or (pe == 8 and n <= 256)
+         or (pe == 4 and n <= 128)]
+
+
+@pytest.mark.parametrize("prec", ["s", "d"])
+@pytest.mark.parametrize("fmt", [1, 3])
+@pytest.mark.parametrize("n,pe", SHORT)
+def test_short_line_plans_give_the_same_transform(prec, fmt, n, pe):
+    import gbfft
+    for shape in [(n, 12, 10), (14, n, 6), (10, 8, n)]:
+        nx, ny, nz = shape
+        x = np.random.default_rng(n + pe + fmt).standard_normal((nz, ny, nx))
+        e = gbfft.Engine(fmt, nx, ny, nz, prec=gbfft.PREC_SINGLE if prec == "s" else gbfft.PREC_DOUBLE)
+        axis = shape.index(n)
+        e.set_plan(axis, pe)
+        assert e.tuning()["points"][axis] == pe
+        tol = 2e-6 if prec == "s" else 1e-12
+        xd = torch.from_numpy(x.astype(np.float32 if prec == "s" else np.float64)).cuda()
+        s = e.empty_spectral()
+        e.r2c(xd, s)
+        assert rel(s.cpu().numpy(), O.fft3d_r2c(x, fmt)) <= tol, shape
+        y = e.empty_physical()
+        e.c2r(s, y)
+        assert rel(y.cpu().numpy() / (nx * ny * nz), x) <= tol, shape
+        c = x + 1j * np.random.default_rng(3).standard_normal(x.shape)
+        cd = torch.from_numpy(c.astype(np.complex64 if prec == "s" else np.complex128)).cuda()
+        o = torch.empty_like(cd)
+        e.c2c(cd, o, -1)
+        assert rel(o.cpu().numpy(), O.fft3d_c2c(c, fmt, O.FORWARD)) <= tol, shape
+        e.close()
+
+
+def test_small_grid_engines_choose_short_plans_and_batch_keeps_its_own():
+    """A 64^3 engine picks 4 points a thread (its grid cannot fill the GPU at
+    16); a batch of such engines still runs the persistent kernel, which
+    needs the 16-point plan's table, and gives the oracle's spectra."""
+    import gbfft
+    e = gbfft.Engine(1, 64, 64, 64, prec=gbfft.PREC_SINGLE)
+    assert e.tuning()["points"] == (4, 4, 4)
+    e.close()
+    grids = [(64, 32, 48, 1), (32, 64, 64, 3), (128, 32, 32, 1)]
+    engines, xs, specs, reals = [], [], [], []
+    b = gbfft.Batch()
+    for nx, ny, nz, fmt in grids:
+        eng = gbfft.Engine(fmt, nx, ny, nz, prec=gbfft.PREC_SINGLE)
+        x = np.random.default_rng(nx + ny).standard_normal((nz, ny, nx))
+        xd = torch.from_numpy(x.astype(np.float32)).cuda()
+        s = eng.empty_spectral()
+        b.add(eng, xd, s)
+        engines.append(eng)
+        xs.append((x, fmt))
+        specs.append(s)
+        reals.append(xd)
+    assert b.info()["persistent"]
+    b.run(1)
+    torch.cuda.synchronize()
+    b.status()
+    for (x, fmt), s in zip(xs, specs):
+        assert rel(s.cpu().numpy(), O.fft3d_r2c(x, fmt)) <= 2e-6
+    b.close()
+    for eng in engines:
+        eng.close()

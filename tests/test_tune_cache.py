@@ -20,7 +20,7 @@ def allowed(key, v):
     if key in ("flat", "tma"):
         return v in (0, 1)
     if key in ("e_x", "e_y", "e_z"):
-        return v in (2, 9, 16, 20, 24, 30, 32)
+        return v in (2, 4, 8, 9, 16, 20, 24, 30, 32)
     m = re.fullmatch(r"(cl_|cls_)?(\w+)", key)
     if not m or m.group(2) not in PASSES:
         return False
