@@ -726,12 +726,23 @@ Pass c2c_pass(const gbfft_engine_s* e, int axis, int n1, int n2, int n3, const v
     }
   }
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, K_C2C, e->tile_L[GBFFT_PASS_C2C_X + axis],
-            e->form == GBFFT_FORM_SPLIT, e->csize[GBFFT_PASS_C2C_X + axis],
+            e->form != GBFFT_FORM_PLAIN, e->csize[GBFFT_PASS_C2C_X + axis],
             e->csync[GBFFT_PASS_C2C_X + axis]);
   // 1024-point FP32 y passes over rows a tensor map can describe: the
   // persistent kernel whose tiles arrive by bulk tensor copies (its plan
   // shares the axis's stage-major twiddle table).  Shorter lines and z
   // passes stay on the one-shot kernel, which is as fast or faster there.
+  // the tcgen05 form: strided 1024-point c2c passes on the 5th-generation
+  // tensor cores (its DFT matrix and twiddles come from the n-root table)
+  if (e->form == GBFFT_FORM_SPLIT_TC && e->d_status && a.fast == 3) {
+    PassArgs t = a;
+    t.tw = e->ax[axis].d_tw;
+    if (tc_pass_supported(e->prec, K_C2C, P.contiguous, t)) {
+      a.tw = t.tw;
+      a.fast = 5;
+      a.status = e->d_status;
+    }
+  }
   if (e->tma && e->d_status && axis == 1 && a.fast == 1 && tma_pass_supported(e->prec, K_C2C, P.contiguous, a)) {
     a.tma = 1;
     a.status = e->d_status;
@@ -810,7 +821,7 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst, lo
     a.pair_vec |= 2;
   const int axis = e->format == GBFFT_PHYSICAL_IN_X ? 0 : 2;
   fill_plan(a, e->ax[axis], e->prec, P.contiguous, kind,
-            e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R], e->form == GBFFT_FORM_SPLIT,
+            e->tile_L[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R], e->form != GBFFT_FORM_PLAIN,
             e->csize[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R],
             e->csync[kind == K_R2C ? GBFFT_PASS_R2C : GBFFT_PASS_C2R]);
   P.big = e->ax[axis].big;
@@ -824,7 +835,7 @@ Pass real_pass(const gbfft_engine_s* e, int kind, const void* src, void* dst, lo
 // by one fused x/y kernel when one exists for the lengths.  `planes` is the
 // z extent of the array the two passes work on.
 void fuse_xy(const gbfft_engine_s* e, std::vector<Pass>& ps, long long planes) {
-  if (!e->d_sync || planes > e->sync_planes || e->form == GBFFT_FORM_SPLIT) return;
+  if (!e->d_sync || planes > e->sync_planes || e->form != GBFFT_FORM_PLAIN) return;
   for (size_t i = 0; i + 1 < ps.size(); ++i) {
     Pass& p0 = ps[i];
     Pass& p1 = ps[i + 1];
@@ -950,9 +961,9 @@ int check_engine_args(int format, int nx, int ny, int nz, int prec, int form) {
     return fail(GBFFT_ERR_INVALID, "Invalid value for pencil");
   if (prec != GBFFT_PREC_SINGLE && prec != GBFFT_PREC_DOUBLE)
     return fail(GBFFT_ERR_INVALID, "Invalid value for precision (4 or 8)");
-  if (form != GBFFT_FORM_PLAIN && form != GBFFT_FORM_SPLIT)
+  if (form != GBFFT_FORM_PLAIN && form != GBFFT_FORM_SPLIT && form != GBFFT_FORM_SPLIT_TC)
     return fail(GBFFT_ERR_INVALID, "Invalid value for form");
-  if (form == GBFFT_FORM_SPLIT && prec != GBFFT_PREC_SINGLE)
+  if (form != GBFFT_FORM_PLAIN && prec != GBFFT_PREC_SINGLE)
     return fail(GBFFT_ERR_UNSUPPORTED, "the split tensor-core form works on single-precision data");
   const long long cells = (long long)nx * ny * nz;
   if (cells > (1LL << 40)) return fail(GBFFT_ERR_UNSUPPORTED, "grid too large");
@@ -1004,7 +1015,7 @@ int engine_init_host(gbfft_engine_s* e, int format, int nx, int ny, int nz, int 
     if (fast_has_alt(lens[d]) && tune.e[d] > 0 && fast_e_ok(lens[d], tune.e[d])) e->ax[d].fast_e = tune.e[d];
     if (gen_length(lens[d]) && (tune.e[d] == gen_points(lens[d]) || tune.e[d] == 2))
       e->ax[d].fast_e = tune.e[d];
-    if (form == GBFFT_FORM_SPLIT && split_length(lens[d])) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
+    if (form != GBFFT_FORM_PLAIN && split_length(lens[d])) e->ax[d].fast_e = 16;  // radix-16 stages for the tensor cores
   }
   *tune_out = tune;
   return GBFFT_OK;
@@ -1174,6 +1185,7 @@ int gbfft_version(int* major, int* minor) {
 long long gbfft_launch_count(void) { return launch_counter(); }
 
 long long gbfft_tma_pass_count(void) { return tma_launch_counter(); }
+long long gbfft_tc_pass_count(void) { return tc_launch_counter(); }
 
 int gbfft_debug_fail_alloc(long long nth) {
   if (nth < -1) return fail(GBFFT_ERR_INVALID, "bad argument");
@@ -1544,7 +1556,7 @@ int gbfft_engine_set_plan(gbfft_engine_t e, int axis, int points) {
   if (!valid_engine(e)) return fail(GBFFT_ERR_INVALID, "not an engine");
   if (axis < 0 || axis > 2) return fail(GBFFT_ERR_INVALID, "bad axis");
   AxisPlan& p = e->ax[axis];
-  if (e->form == GBFFT_FORM_SPLIT && split_length(p.n))
+  if (e->form != GBFFT_FORM_PLAIN && split_length(p.n))
     return fail(GBFFT_ERR_UNSUPPORTED, "the split form has one plan");
   if (gen_length(p.n)) {
     if (points != gen_points(p.n) && points != 2)

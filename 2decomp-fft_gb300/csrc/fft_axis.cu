@@ -161,6 +161,10 @@ cudaError_t launch_axis_one(int prec_bytes, int kind, bool contiguous, const Pas
     if (!tma_pass_supported(prec_bytes, kind, contiguous, a)) return cudaErrorInvalidValue;
     return launch_tma_pass(a, stream);
   }
+  if (a.fast == 5) {
+    if (!tc_pass_supported(prec_bytes, kind, contiguous, a)) return cudaErrorInvalidValue;
+    return launch_tc_pass(a, stream);
+  }
   if (a.fast == 4) return prec_bytes == 4 ? launch_gen_f32(kind, contiguous, a, stream)
                                           : launch_gen_f64(kind, contiguous, a, stream);
   if (a.fast == 3) {

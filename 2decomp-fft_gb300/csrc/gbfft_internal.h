@@ -77,8 +77,9 @@ struct PassArgs {
   int first_fused; // stage 0 reads global memory directly
   int last_fused;  // last stage writes global memory directly
   int fast;        // 1: compile-time power-of-two kernel, 2: mixed-radix kernel,
-                   // 3: split-precision tensor-core kernel, 4: balanced
-                   // non-power-of-two plan
+                   // 3: split-precision tensor-core kernel (mma.sync), 4:
+                   // balanced non-power-of-two plan, 5: split-precision
+                   // tcgen05 kernel (fft_tc.cu)
   int pair_vec;    // r2c/c2r on strided lines, bit 0: the two real lines of a
                    // pair are adjacent and aligned (read/write as one pair);
                    // bit 1 (FP32): so are their two complex lines, 16-byte
@@ -300,6 +301,13 @@ cudaError_t launch_dtt_pass(int prec_bytes, bool contiguous, const DttArgs& a, c
 bool tma_pass_supported(int prec_bytes, int kind, bool contiguous, const PassArgs& a);
 cudaError_t launch_tma_pass(const PassArgs& a, cudaStream_t stream);
 long long tma_launch_counter();
+
+// Split-precision strided c2c passes of 1024 FP32 points on tcgen05 with
+// TMEM accumulators (fft_tc.cu): a.fast == 5, a.tw the n-root table,
+// a.status the engine's status word.
+bool tc_pass_supported(int prec_bytes, int kind, bool contiguous, const PassArgs& a);
+cudaError_t launch_tc_pass(const PassArgs& a, cudaStream_t stream);
+long long tc_launch_counter();
 
 // Axis passes whose lines do not fit one shared-memory tile, or whose
 // length has a prime factor above kBluePrime (fft_long.cu): one kernel per

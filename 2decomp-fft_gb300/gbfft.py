@@ -35,6 +35,7 @@ PREC_SINGLE = 4
 PREC_DOUBLE = 8
 FORM_PLAIN = 0
 FORM_SPLIT = 1
+FORM_SPLIT_TC = 2
 X_TO_Y, Y_TO_Z, Z_TO_Y, Y_TO_X = 0, 1, 2, 3
 PASS_NAMES = ["r2c", "c2r", "c2c_x", "c2c_y", "c2c_z", "xy_fused"]
 D2D_FFT_BACKEND = 5
@@ -98,6 +99,7 @@ SIGNATURES = {
     "gbfft_version": (_i, [_ip, _ip]),
     "gbfft_launch_count": (ctypes.c_longlong, []),
     "gbfft_tma_pass_count": (ctypes.c_longlong, []),
+    "gbfft_tc_pass_count": (ctypes.c_longlong, []),
     "gbfft_engine_set_tma": (_i, [_vp, _i]),
     "gbfft_engine_get_tma": (_i, [_vp, _ip]),
     # decomp_2d_fft.h
@@ -173,6 +175,11 @@ def check(status):
 
 def launch_count():
     return int(lib().gbfft_launch_count())
+
+
+def tc_pass_count():
+    """gbfft_tc_pass_count: tcgen05 split-precision passes launched so far."""
+    return int(lib().gbfft_tc_pass_count())
 
 
 def tma_pass_count():

@@ -415,7 +415,7 @@ def run_gb300(args):
     rdt = torch.float32 if prec == 4 else torch.float64
     gbfft.lib()
 
-    form = gbfft.FORM_SPLIT if args.form == "split" else gbfft.FORM_PLAIN
+    form = {"split": gbfft.FORM_SPLIT, "split_tc": gbfft.FORM_SPLIT_TC}.get(args.form, gbfft.FORM_PLAIN)
     eng = gbfft.Engine(fmt, nx, ny, nz, prec=prec, form=form)
     x = make_input(nx, ny, nz, kind, rdt, dev)
     spec = eng.empty_spectral(device=dev)
@@ -964,8 +964,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
                     choices=sorted(WORKLOADS) + [BATCH_WORKLOAD] + sorted(DTT_WORKLOADS))
-    ap.add_argument("--form", default="plain", choices=["plain", "split"],
-                    help="plain FP32/FP64 stages, or split-FP16 tensor-core radix-16 stages (FP32 only)")
+    ap.add_argument("--form", default="plain", choices=["plain", "split", "split_tc"],
+                    help="plain FP32/FP64 stages, split-FP16 tensor-core radix-16 stages on mma.sync (split), "
+                         "or with the strided 1024-point passes on tcgen05 (split_tc); FP32 only")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,

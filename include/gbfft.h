@@ -51,6 +51,10 @@ extern "C" {
 #define GBFFT_FORM_SPLIT 1 /* radix-16 stages as split-FP16 tensor-core DFTs
                               (FP32 data; axes of 256, 512, 1024 points; other
                               axes run the plain kernels) */
+#define GBFFT_FORM_SPLIT_TC 2 /* as GBFFT_FORM_SPLIT, with strided 1024-point
+                                 c2c passes as two 32-point split-FP16 DFT
+                                 products on the 5th-generation tensor cores
+                                 (tcgen05, accumulators in tensor memory) */
 
 /* transpose kinds (src/decomp_2d.f90:140-222 generic transpose_* names) */
 #define GBFFT_X_TO_Y 0
@@ -70,7 +74,8 @@ typedef struct gbfft_engine_s* gbfft_engine_t;
  *           (opt_skip_XYZ_c2c; r2c/c2r along the real axis cannot be skipped
  *           and only warns, as src/fft_generic.f90:221-222 does)
  *   prec    GBFFT_PREC_SINGLE or GBFFT_PREC_DOUBLE
- *   form    GBFFT_FORM_PLAIN or GBFFT_FORM_SPLIT (SPLIT needs PREC_SINGLE) */
+ *   form    GBFFT_FORM_PLAIN, GBFFT_FORM_SPLIT or GBFFT_FORM_SPLIT_TC (both split
+ *           forms need PREC_SINGLE) */
 int gbfft_engine_create(int format, int nx, int ny, int nz, int inplace,
                         const int* skip, int prec, int form,
                         gbfft_engine_t* engine);
@@ -422,6 +427,9 @@ long long gbfft_launch_count(void);
 /* Of those, the strided passes run by the bulk-tensor-copy kernel
  * (gbfft_engine_set_tma). */
 long long gbfft_tma_pass_count(void);
+/* Number of tcgen05 split-precision passes launched so far, process-wide
+ * (GBFFT_FORM_SPLIT_TC engines); no counterpart in the reference. */
+long long gbfft_tc_pass_count(void);
 
 /* ---- real-to-real transforms (DCT / DST) ----------------------------------
  * decomp_2d_dtt_3d_r2r and the opt_DTT configuration of decomp_2d_fft_init
