@@ -242,8 +242,11 @@ __global__ void __launch_bounds__(kThreads, 2) tc_pass_kernel(const __grid_const
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a)
                      : "memory");
       }
-      const bool got = mbar_wait(bar_a, phase);
-      if (__syncthreads_or(!got)) {  // one decision for the whole CTA
+      // one thread polls the mbarrier (every thread polling would take the
+      // shared-memory pipe and issue slots from the SM's other CTA); the
+      // barrier releases the rest and carries the decision to all of them
+      const bool got = t == 0 ? mbar_wait(bar_a, phase) : true;
+      if (__syncthreads_or(!got)) {
         ok = false;
         if (t == 0 && a.status) atomicExch(a.status, 1);
         break;
