@@ -40,7 +40,7 @@ constexpr int tile_lines() {
 template <typename T, int KIND, bool CONTIG, int N>
 __device__ __forceinline__ void run_tile(const BatchDesc& D, Cx<T>* Sm, long long tile) {
   constexpr bool MIXED = !((N & (N - 1)) == 0);
-  constexpr int TPL = MIXED ? N / mixed_r0(N) : N / fast_points(N, CONTIG);
+  constexpr int TPL = MIXED ? N / mixed_r0(N) : N / batch_points(N);
   constexpr int LE = tile_lines<TPL>();
   const int tid = threadIdx.x;
   int t, line;
@@ -69,7 +69,7 @@ __device__ __forceinline__ void run_tile(const BatchDesc& D, Cx<T>* Sm, long lon
   if constexpr (MIXED) {
     mixed::run_mixed<N>(c, Sm);
   } else {
-    constexpr int E = fast_points(N, CONTIG);
+    constexpr int E = batch_points(N);
     Cx<T> v[E];
     fast::run_stages<N, E, 0>(c, Sm, v);
     if constexpr (KIND == K_R2C) c.store_r2c_pairs(Sm);
@@ -158,7 +158,8 @@ bool batch_length(int n) {
 
 int batch_tile_lines(int n, bool contiguous) {
   const bool mixed = (n & (n - 1)) != 0;
-  const int tpl = mixed ? n / mixed_r0(n) : n / fast_points(n, contiguous);
+  const int tpl = mixed ? n / mixed_r0(n) : n / batch_points(n);
+  (void)contiguous;
   return kBT / tpl;
 }
 

@@ -90,8 +90,8 @@ struct AxisPlan {
                       // of fft_long.cu (implies big)
   void* d_tw = nullptr;   // exp(-2 pi i m / n), m = 0..n-1
   void* d_twf = nullptr;  // stage-major table of the power-of-two kernel
-  void* d_twf16 = nullptr;  // the same for 16 points a thread, when the axis
-                            // runs 4 or 8 (the batch kernel's plan)
+  void* d_twfb = nullptr;   // the same for the batch kernel's plan
+                            // (batch_points), when the axis runs another
   void* d_chirp = nullptr;  // chirp-z tables (bt points at them)
   void* d_filt = nullptr;
   void* d_twm = nullptr;
@@ -303,13 +303,14 @@ int upload_blue(AxisPlan& p, int prec) {
   return GBFFT_OK;
 }
 
-// The batch kernel runs 16 points a thread on power-of-two lines: an axis
-// on 4 or 8 also keeps that plan's stage-major table.
+// The batch kernel runs batch_points(n) points a thread on power-of-two
+// lines of at most 256 points: an axis on another plan also keeps that
+// plan's stage-major table.
 int upload_batch_table(AxisPlan& p, int prec) {
-  if (!fast_length(p.n) || (p.fast_e != 4 && p.fast_e != 8) || p.d_twf16) return GBFFT_OK;
+  if (!fast_length(p.n) || p.n > 256 || p.fast_e == batch_points(p.n) || p.d_twfb) return GBFFT_OK;
   AxisPlan q = p;
-  q.fast_e = 16;
-  return upload_table(&p.d_twf16, stage_twiddles(plan_radices(q)), prec);
+  q.fast_e = batch_points(p.n);
+  return upload_table(&p.d_twfb, stage_twiddles(plan_radices(q)), prec);
 }
 
 int upload_twiddles(AxisPlan& p, int prec) {
@@ -467,7 +468,7 @@ void drop_profile(gbfft_engine_t e) {
 void release(gbfft_engine_t e) {
   drop_profile(e);
   for (auto& a : e->ax) {
-    for (void** q : {&a.d_tw, &a.d_twf, &a.d_twf16, &a.d_chirp, &a.d_filt, &a.d_twm}) {
+    for (void** q : {&a.d_tw, &a.d_twf, &a.d_twfb, &a.d_chirp, &a.d_filt, &a.d_twm}) {
       if (*q) dev_free(*q);
       *q = nullptr;
     }
@@ -1119,12 +1120,12 @@ int gbfft::engine_passes(gbfft_engine_s* e, int which, const void* in, void* out
   if ((int)ps.size() > max_passes) return fail(GBFFT_ERR_INVALID, "too many passes");
   for (size_t i = 0; i < ps.size(); ++i) {
     PassInfo q{ps[i].a, ps[i].kind, ps[i].contiguous};
-    // the batch kernel's power-of-two plan is 16 points a thread
+    // the batch kernel's power-of-two plans are batch_points(n) points a thread
     if (q.a.fast == 1)
       for (const AxisPlan& ax : e->ax)
-        if (q.a.tw == ax.d_twf && ax.d_twf16) {
-          q.a.tw = ax.d_twf16;
-          q.a.tpl = q.a.n / fast_points(q.a.n, q.contiguous);
+        if (q.a.tw == ax.d_twf && ax.d_twfb) {
+          q.a.tw = ax.d_twfb;
+          q.a.tpl = q.a.n / batch_points(q.a.n);
         }
     out_passes[i] = q;
   }
