@@ -268,7 +268,7 @@ int upload_blue(AxisPlan& p, int prec) {
   const int n = p.n;
   long long m = 1;
   while (m < 2LL * n - 1) m <<= 1;
-  if (m > (1LL << 27)) return fail(GBFFT_ERR_UNSUPPORTED, "axis too long for the chirp-z path");
+  if (m > (1LL << 24)) return fail(GBFFT_ERR_UNSUPPORTED, "axis too long for the chirp-z path");
   const long double pi = 3.141592653589793238462643383279502884L;
   std::vector<double> w(2 * (size_t)n), b(2 * (size_t)m, 0.0);
   for (long long j = 0; j < n; ++j) {
@@ -1001,7 +1001,9 @@ int engine_init_host(gbfft_engine_s* e, int format, int nx, int ny, int nz, int 
     e->ax[d].big = lens[d] > kMaxN || pass_smem_bytes(prec, lens[d], 1) > 200 * 1024;
     // a large prime factor: the chirp-z transform (O(n log n)) instead of a
     // direct-sum stage (O(p) a point)
-    e->ax[d].blue = largest_prime(e->ax[d]) > kBluePrime;
+    // (up to convolutions of 2^24 points: the host tables take 32 bytes a
+    // point; longer axes keep the direct-sum stages)
+    e->ax[d].blue = largest_prime(e->ax[d]) > kBluePrime && 2LL * lens[d] - 1 <= (1LL << 24);
     if (e->ax[d].blue) e->ax[d].big = true;
     e->ax[d].fast_e = fast_points(lens[d], d == 0);  // axis 0 runs contiguous lines
     if (fast_length(lens[d]) && lens[d] <= 256) {
