@@ -62,6 +62,10 @@ DEFAULT_WORKLOAD = "r2c_c2r_1024x1024x512_f32_x"
 BATCH_WORKLOAD = "batched_64_grids_f32"
 # real-to-real (DCT-II on every axis, default windows: the last point of each
 # axis left out) forward + backward: name -> (nx, ny, nz, precision, kinds)
+# transposes plus c2c: the x -> y -> z -> y -> x transpose chain on a 256^3
+# real64 and complex128 array (at one rank each transpose is an identity
+# copy, bit for bit), then a 3D c2c forward + backward in complex64
+C2C_WORKLOAD = "c2c_transposes_256x256x256"
 DTT_WORKLOADS = {
     "r2r_dct2_256x256x256_f64_x": (256, 256, 256, 8, (2, 2, 2)),
     "r2r_dct2_256x256x256_f32_x": (256, 256, 256, 4, (2, 2, 2)),
@@ -917,6 +921,177 @@ def run_dtt(args):
     return out
 
 
+def run_c2c_chain(args):
+    """Transposes plus c2c on 256^3: one step = a complex64 c2c forward +
+    backward through the C ABI (value, GPts/s); beside it the four one-rank
+    transposes (x->y->z->y->x) on real64 and complex128 arrays, timed as
+    copies (GB/s against the copy peak) and checked bit for bit."""
+    import torch
+    import numpy as np
+    import gbfft
+    from oracle import oracle as O
+    world, rank, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n = 256
+    npts = n ** 3
+    gbfft.lib()
+    stream = torch.cuda.current_stream(dev)
+    rng = np.random.default_rng(9)
+    a = (rng.uniform(-1, 1, (n, n, n)) + 1j * rng.uniform(-1, 1, (n, n, n))).astype(np.complex64)
+    x = torch.from_numpy(a).to(dev)
+    y = torch.empty_like(x)
+    eng = gbfft.Engine(gbfft.PHYSICAL_IN_X, n, n, n, prec=gbfft.PREC_SINGLE)
+
+    def step():
+        eng.c2c(x, y, gbfft.FORWARD, stream)
+        eng.c2c(y, x, gbfft.BACKWARD, stream)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    x.copy_(torch.from_numpy(a))
+    barrier()
+    torch.cuda.synchronize()
+    l0 = gbfft.launch_count()
+    t_wall0 = time.time()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    barrier()
+    launches = gbfft.launch_count() - l0
+    # per-pass device times, in steps of their own (events recorded by the library)
+    prof_steps = max(1, min(args.steps, 10))
+    eng.set_profiling(True)
+    for _ in range(prof_steps):
+        step()
+    torch.cuda.synchronize()
+    prof = eng.profile()
+    eng.set_profiling(False)
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    value = sum_over_ranks(npts) / (ms * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs") or 6800.0
+    bytes_step = 6 * 2 * npts * 8  # six passes, each one read and one write of the complex64 array
+    # the transpose chain, real64 and complex128 (4 identity copies each)
+    chains = {}
+    reps = max(3, min(args.steps, 20))
+    for name, dt, cplx in (("real64", torch.float64, 0), ("complex128", torch.complex128, 1)):
+        src = torch.from_numpy(rng.uniform(-1, 1, (n, n, n))).to(dt).to(dev) if not cplx else \
+            torch.from_numpy(rng.uniform(-1, 1, (n, n, n)) + 1j * rng.uniform(-1, 1, (n, n, n))).to(dt).to(dev)
+        bufs = [torch.empty_like(src) for _ in range(4)]
+
+        def chain():
+            seq = [src] + bufs
+            for k, kind in enumerate((gbfft.X_TO_Y, gbfft.Y_TO_Z, gbfft.Z_TO_Y, gbfft.Y_TO_X)):
+                gbfft.transpose(kind, seq[k], seq[k + 1], n, n, n, cplx, gbfft.PREC_DOUBLE, stream)
+
+        for _ in range(3):
+            chain()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            chain()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        cms = max_over_ranks(e0.elapsed_time(e1) / reps)
+        cbytes = 4 * 2 * src.numel() * src.element_size()
+        chains[name] = {"ms_per_chain": round(cms, 4), "gbs": round(cbytes / (cms * 1e-3) / 1e9, 1),
+                        "frac": round(cbytes / (cms * 1e-3) / 1e9 / peak, 4), "bytes_per_chain": cbytes,
+                        "bit_exact": bool(torch.equal(bufs[-1], src))}
+    # end to end: input from pinned host memory, result back, every step
+    xh = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+    xh.copy_(torch.from_numpy(a))
+    yh = torch.empty_like(xh, pin_memory=True)
+
+    def e2e_step():
+        x.copy_(xh, non_blocking=True)
+        eng.c2c(x, y, gbfft.FORWARD, stream)
+        eng.c2c(y, x, gbfft.BACKWARD, stream)
+        yh.copy_(x, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / reps)
+    clocks.stop()
+    out = None
+    if rank == 0:
+        acc = {}
+        if not args.no_accuracy:
+            x.copy_(torch.from_numpy(a))
+            eng.c2c(x, y, gbfft.FORWARD, stream)
+            torch.cuda.synchronize()
+            ref = np.fft.fftn(a.astype(np.complex128))
+            acc["rel_l2_vs_fp64"] = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
+            acc["fp64_reference"] = "numpy pocketfft FP64 on the same input"
+        cpu = None
+        if not args.no_cpu:
+            threads = O.set_threads(os.cpu_count() or 1)
+            O.fft3d_c2c(a, O.PHYSICAL_IN_X, O.FORWARD, prec="s")  # warm-up
+            t0 = time.time()
+            r = 0
+            while r < 2:
+                f = O.fft3d_c2c(a, O.PHYSICAL_IN_X, O.FORWARD, prec="s")
+                O.fft3d_c2c(f, O.PHYSICAL_IN_X, O.BACKWARD, prec="s")
+                r += 1
+            dt = (time.time() - t0) / r
+            cpu = {"value": round(npts / dt / 1e9, 5), "unit": "GPts/s", "cores": threads, "kind": "port",
+                   "ms_per_round_trip": round(dt * 1e3, 1),
+                   "sample": "oracle (restated generic backend, single build), OpenMP over lines: whole c2c "
+                             "forward + backward round trips of the full grid, 1 warm-up then the mean of 2"}
+        passes = {}
+        for k, (nl, tms, by) in prof.items():
+            per = tms / nl
+            passes[k] = {"launches_per_step": nl / prof_steps, "ms_per_launch": round(per, 4),
+                         "gbs": round(by / (tms * 1e-3) / 1e9, 1), "bytes_per_launch": by / nl}
+        dom = max(passes, key=lambda k: passes[k]["ms_per_launch"] * passes[k]["launches_per_step"]) \
+            if passes else None
+        out = {
+            "metric": "3D c2c forward+backward GPts/s (complex64) & %HBM roofline; transpose chain bit-exact",
+            "value": round(value, 3), "unit": "GPts/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded uniform [-1,1) real and imaginary parts",
+            "config": {"workload": "transposes x->y->z->y->x (real64, complex128) then c2c forward+backward "
+                                   "256x256x256 complex64", "name": args.workload, "nx": n, "ny": n, "nz": n,
+                       "l2": "arrays of 134-268 MB, around the 129 MB L2 (no flush)",
+                       "parallelism": "replicas (one grid per GPU)"},
+            "roofline": {"bound": "hbm", "kernel": ("axis pass %s" % dom) if dom else "six c2c axis passes",
+                         "achieved": passes[dom]["gbs"] if dom else None, "peak": peak, "unit": "GB/s",
+                         "frac": round(passes[dom]["gbs"] / peak, 4) if dom else None, "traffic": None,
+                         "step_frac": round(bytes_step / (ms * 1e-3) / 1e9 / peak, 4),
+                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"},
+            "passes": passes,
+            "transposes": chains,
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(npts / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GPts/s",
+                    "ms_per_step": round(e2e_ms, 3),
+                    "h2d_bytes_per_step": x.numel() * x.element_size(),
+                    "d2h_bytes_per_step": x.numel() * x.element_size()},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(t_wall0, t_wall1),
+            "accuracy": acc,
+        }
+        print(json.dumps(out), flush=True)
+    eng.close()
+    return out
+
+
 def run_reference(args):
     """The reference arm: the reference's CPU path for this workload -- the
     oracle, a restatement of its generic backend (the Fortran reference
@@ -963,7 +1138,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD] + sorted(DTT_WORKLOADS))
+                    choices=sorted(WORKLOADS) + [BATCH_WORKLOAD, C2C_WORKLOAD] + sorted(DTT_WORKLOADS))
     ap.add_argument("--form", default="plain", choices=["plain", "split", "split_tc"],
                     help="plain FP32/FP64 stages, split-FP16 tensor-core radix-16 stages on mma.sync (split), "
                          "or with the strided 1024-point passes on tcgen05 (split_tc); FP32 only")
@@ -982,6 +1157,8 @@ def main():
         run_batched(args)
     elif args.workload in DTT_WORKLOADS:
         run_dtt(args)
+    elif args.workload == C2C_WORKLOAD:
+        run_c2c_chain(args)
     else:
         run_gb300(args)
 
