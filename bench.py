@@ -545,18 +545,25 @@ def run_gb300(args):
     y2 = [y, torch.empty_like(y)]
     yh2 = [yh, torch.empty_like(yh, pin_memory=True)]
 
+    copy_ms = {"h2d": [], "d2h": []}
+
     def pipelined(nsteps, t0=None, t1=None):
         ev_in = [torch.cuda.Event() for _ in range(nsteps)]
         ev_comp = [torch.cuda.Event() for _ in range(nsteps)]
         ev_out = [torch.cuda.Event() for _ in range(nsteps)]
+        # every copy's own duration: the link bandwidth this window really got
+        c_in = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+        c_out = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
         if t0 is not None:
             t0.record(s_in)
         for i in range(nsteps):
             b = i % 2
             if i >= 2:
                 s_in.wait_event(ev_comp[i - 2])  # xd2[b] read by step i-2
+            c_in[i][0].record(s_in)
             with torch.cuda.stream(s_in):
                 xd2[b].copy_(xh, non_blocking=True)
+            c_in[i][1].record(s_in)
             ev_in[i].record(s_in)
             stream.wait_event(ev_in[i])
             if i >= 2:
@@ -565,12 +572,17 @@ def run_gb300(args):
             eng.c2r(spec, y2[b], stream)
             ev_comp[i].record(stream)
             s_out.wait_event(ev_comp[i])
+            c_out[i][0].record(s_out)
             with torch.cuda.stream(s_out):
                 yh2[b].copy_(y2[b], non_blocking=True)
+            c_out[i][1].record(s_out)
             ev_out[i].record(s_out)
         if t1 is not None:
             s_out.wait_event(ev_comp[nsteps - 1])
             t1.record(s_out)
+        torch.cuda.synchronize()
+        copy_ms["h2d"].append(sum(a.elapsed_time(b) for a, b in c_in) / nsteps)
+        copy_ms["d2h"].append(sum(a.elapsed_time(b) for a, b in c_out) / nsteps)
         return (nsteps - 1) % 2
 
     pipelined(2)
@@ -588,6 +600,9 @@ def run_gb300(args):
         barrier()
         reps.append(max_over_ranks(e0.elapsed_time(e1) / pipe_steps))
     e2e_ms = sorted(reps)[1]
+    med = reps.index(e2e_ms)
+    observed = {k: round(x.numel() * x.element_size() / (v[1 + med] * 1e-3) / 1e9, 1) for k, v in copy_ms.items()}
+    link_after = link_gbs(xh, xd, stream)
     same = bool(torch.equal(yh2[last], yh2[1 - last]))  # deterministic: every step's result alike
     e2e = {"value": round(total_pts / (e2e_ms * 1e-3) / 1e9, 3), "unit": "GPts/s",
            "ms_per_step": round(e2e_ms, 3),
@@ -598,6 +613,8 @@ def run_gb300(args):
            "repetitions_ms": [round(v, 3) for v in reps],
            "results_identical_across_steps": same,
            "host_link_gbs": link,
+           "host_link_gbs_after": link_after,
+           "copy_gbs_during_e2e": observed,
            "host_cpus": "%d CPUs on the GPU's NUMA node (%s)" % (len(cpus), "bound" if gpu_local_cpus(local) else
                                                                  "node unknown: not bound"),
            "link_bound_ms": round(max(x.numel() * x.element_size() / (link["both_each"] * 1e9),
