@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kBT, 4)
   }
 }
 
-int g_grid = 0;
+int g_grid[kMaxDevices] = {0};  // resident CTAs of the batch kernel, per device
 
 // One thread waits for counter[0] >= need with a poll limit (self-test of
 // the bounded wait).
@@ -178,21 +178,25 @@ cudaError_t launch_batch_f32(const BatchDesc* d_desc, const long long* d_prefix,
                              long long sync_ints, cudaStream_t stream) {
   auto kern = batch_kernel<float>;
   const size_t smem = batch_smem_bytes();
-  if (g_grid == 0) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0, dev = 0, sms = 0;
+  // the shared-memory limit is a per-device attribute: set it every launch;
+  // the resident CTA count is cached per device
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (g_grid[dev] == 0) {
+    int per_sm = 0, sms = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBT, smem);
-    if (e != cudaSuccess) return e;
-    e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    g_grid = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    g_grid[dev] = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   }
-  cudaError_t e = cudaMemsetAsync(d_sync, 0, (size_t)sync_ints * sizeof(int), stream);
+  e = cudaMemsetAsync(d_sync, 0, (size_t)sync_ints * sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  kern<<<g_grid, kBT, smem, stream>>>(d_desc, d_prefix, ndesc, d_sync);
+  kern<<<g_grid[dev], kBT, smem, stream>>>(d_desc, d_prefix, ndesc, d_sync);
   add_launches(1);
   return cudaGetLastError();
 }

@@ -141,23 +141,27 @@ template <typename T, int KINDX, bool XFIRST, int NX, int NY, int TH>
 cudaError_t launch(const FusedArgs& f, cudaStream_t stream) {
   auto kern = fused_xy_kernel<T, KINDX, XFIRST, NX, NY, TH>;
   const size_t smem = smem_bytes<NX, NY, TH>((int)sizeof(Cx<T>));
-  static int grid = 0;  // resident CTAs, per instantiation, first use
-  if (grid == 0) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0, dev = 0, sms = 0;
+  // the shared-memory limit is a per-device attribute: set it every launch;
+  // the resident CTA count is cached per device and instantiation
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  static int grid[kMaxDevices] = {0};
+  if (grid[dev] == 0) {
+    int per_sm = 0, sms = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TH, smem);
-    if (e != cudaSuccess) return e;
-    e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    grid = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    grid[dev] = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   }
   const size_t sync_bytes = (size_t)(f.nplanes + 2) * sizeof(int);
-  cudaError_t e = cudaMemsetAsync(f.sync, 0, sync_bytes, stream);
+  e = cudaMemsetAsync(f.sync, 0, sync_bytes, stream);
   if (e != cudaSuccess) return e;
-  kern<<<grid, TH, smem, stream>>>(f);
+  kern<<<grid[dev], TH, smem, stream>>>(f);
   add_launches(1);
   return cudaGetLastError();
 }

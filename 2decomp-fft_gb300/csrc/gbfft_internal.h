@@ -17,6 +17,7 @@ constexpr int kMaxThreads = 512;  // threads in one CTA of an axis pass
 constexpr int kMaxN = 8192;       // longest axis a single-tile pass supports
 constexpr int kMaxGridY = 65535;  // planes (grid.y) of one strided launch
 constexpr int kSmsDefault = 152;  // SMs of a GB300: the occupancy targets of small grids
+constexpr int kMaxDevices = 64;   // per-device caches of launch parameters
 
 // What one axis pass does to each line.
 enum Kind : int {
