@@ -50,6 +50,8 @@ WORKLOADS = {
     "r2c_c2r_1024x1024x128_f32_x": (1024, 1024, 128, 1, 4, "gauss_modes"),
     "r2c_c2r_512x256x512_f32_x": (512, 256, 512, 1, 4, "gauss_modes"),
     "r2c_c2r_1024x64x512_f32_x": (1024, 64, 512, 1, 4, "gauss_modes"),
+    # the PHYSICAL_IN_Z grid's 512-point strided real lines at 1/8 the memory
+    "r2c_c2r_512x256x512_f32_z": (512, 256, 512, 3, 4, "gauss_modes"),
     # axis lengths off the fast paths: the largest prime one shared-memory tile
     # takes (a direct-sum stage), a power of two beyond one tile (one radix
     # stage per kernel through scratch), a prime beyond one tile (a global
