@@ -101,3 +101,31 @@ def test_large_fp32_grid_matches_the_exact_spectrum(fmt):
     d = back.double() / (nx * ny * nz) - x.double()
     assert float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(x.double())) <= 2e-6
     e.close()
+
+
+@pytest.mark.parametrize("form", ["split", "split_tc"])
+def test_large_fp32_grid_split_forms_within_1e6(form):
+    """The split-precision forms at the benchmark's 1024 x 1024 x 512 FP32
+    grid (PHYSICAL_IN_X): the forward spectrum within rel-L2 1e-6 of the exact
+    one (the benchmark spec's bar for a split form), and the round trip."""
+    import gbfft
+    nx, ny, nz = 1024, 1024, 512
+    f = gbfft.FORM_SPLIT if form == "split" else gbfft.FORM_SPLIT_TC
+    before = gbfft.tc_pass_count()
+    e = gbfft.Engine(G.PHYSICAL_IN_X, nx, ny, nz, prec=4, form=f)
+    x = _field(nx, ny, nz, 4)
+    spec = e.empty_spectral()
+    e.r2c(x, spec)
+    torch.cuda.synchronize()
+    exact = _exact_dev(nx, ny, nz, G.PHYSICAL_IN_X)
+    assert _rel(spec, exact) <= 1e-6
+    del exact
+    back = e.empty_physical()
+    e.c2r(spec, back)
+    torch.cuda.synchronize()
+    d = back.double() / (nx * ny * nz) - x.double()
+    assert float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(x.double())) <= 2e-6
+    if form == "split_tc":
+        assert gbfft.tc_pass_count() >= before + 2  # both y passes ran on tcgen05
+    e.status()
+    e.close()
