@@ -207,7 +207,8 @@ cudaError_t launch_axis_one(int prec_bytes, int kind, bool contiguous, const Pas
 // number of planes itself.
 cudaError_t launch_axis_pass(int prec_bytes, int kind, bool contiguous, const PassArgs& a,
                              cudaStream_t stream) {
-  if (contiguous || a.tma || a.nv <= kMaxGridY) return launch_axis_one(prec_bytes, kind, contiguous, a, stream);
+  if (contiguous || a.tma || a.fast == 5 || a.nv <= kMaxGridY)  // persistent kernels take any plane count
+    return launch_axis_one(prec_bytes, kind, contiguous, a, stream);
   const size_t cs = 2 * (size_t)prec_bytes, rs = (size_t)prec_bytes;
   const size_t src_e = kind == K_R2C ? rs : cs, dst_e = kind == K_C2R ? rs : cs;
   for (long long v0 = 0; v0 < a.nv; v0 += kMaxGridY) {

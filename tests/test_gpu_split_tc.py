@@ -1,13 +1,12 @@
 """GPU: the tcgen05 split-precision form (GBFFT_FORM_SPLIT_TC).  Strided
-1024-point c2c passes run as two 32-point DFT products on the 5th-generation
-tensor cores (FP16 hi + lo operands in shared memory, FP32 accumulators in
-tensor memory); the other passes run as in the mma.sync split form.  Every
-case against the FP64 oracle at rel-L2 <= 1e-6 (the benchmark spec's bar for a
-split form), with the tcgen05 kernel's launch counter showing it ran:
-r2c / c2r in both formats with ragged line counts (a tile of 4 lines
-partly past the array), c2c forward and backward along y and z, in place.
-(z passes into rows that are not whole 16-value multiples take each plane
-flat and stay on the mma.sync kernel, so the z case has 16-value rows.)"""
+c2c passes of 1024 points run as two 32-point DFT products on the
+5th-generation tensor cores (FP16 hi + lo operands in shared memory, FP32
+accumulators in tensor memory); the other passes run as in the mma.sync
+split form.  Every case against the FP64 oracle at rel-L2
+<= 1e-6 (the benchmark spec's bar for a split form), with the tcgen05 kernel's
+launch counter showing it ran: r2c / c2r in both formats with ragged line
+counts (a tile of 4 lines partly past the array), per-row and flat-plane z
+passes, c2c forward and backward along y and z, in place."""
 import numpy as np
 import pytest
 
@@ -29,7 +28,8 @@ def _engine(fmt, nx, ny, nz):
 
 
 @pytest.mark.parametrize("fmt,shape", [(O.PHYSICAL_IN_X, (66, 1024, 12)), (O.PHYSICAL_IN_Z, (66, 1024, 10)),
-                                       (O.PHYSICAL_IN_X, (30, 12, 1024)), (O.PHYSICAL_IN_X, (256, 1024, 64))])
+                                       (O.PHYSICAL_IN_X, (30, 12, 1024)), (O.PHYSICAL_IN_X, (256, 1024, 64)),
+                                       (O.PHYSICAL_IN_X, (34, 12, 1024)), (O.PHYSICAL_IN_X, (128, 1024, 256))])
 def test_tc_form_r2c_c2r(fmt, shape):
     import gbfft
     nx, ny, nz = shape
@@ -49,7 +49,7 @@ def test_tc_form_r2c_c2r(fmt, shape):
     e.close()
 
 
-@pytest.mark.parametrize("shape", [(32, 1024, 8), (16, 8, 1024), (6, 1024, 5)])
+@pytest.mark.parametrize("shape", [(32, 1024, 8), (16, 8, 1024), (6, 1024, 5), (5, 4, 1024)])
 def test_tc_form_c2c(shape):
     import gbfft
     nx, ny, nz = shape
