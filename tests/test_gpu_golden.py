@@ -107,7 +107,7 @@ def test_large_fp32_grid_matches_the_exact_spectrum(fmt):
 def test_large_fp32_grid_split_forms_within_1e6(form):
     """The split-precision forms at the benchmark's 1024 x 1024 x 512 FP32
     grid (PHYSICAL_IN_X): the forward spectrum within rel-L2 1e-6 of the exact
-    one (the benchmark spec's bar for a split form), and the round trip."""
+    one (the accuracy bar a split-precision form must meet), and the round trip."""
     import gbfft
     nx, ny, nz = 1024, 1024, 512
     f = gbfft.FORM_SPLIT if form == "split" else gbfft.FORM_SPLIT_TC

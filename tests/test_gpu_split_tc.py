@@ -3,7 +3,7 @@ c2c passes of 1024 points run as two 32-point DFT products on the
 5th-generation tensor cores (FP16 hi + lo operands in shared memory, FP32
 accumulators in tensor memory); the other passes run as in the mma.sync
 split form.  Every case against the FP64 oracle at rel-L2
-<= 1e-6 (the benchmark spec's bar for a split form), with the tcgen05 kernel's
+<= 1e-6 (the accuracy bar a split-precision form must meet), with the tcgen05 kernel's
 launch counter showing it ran: r2c / c2r in both formats with ragged line
 counts (a tile of 4 lines partly past the array), per-row and flat-plane z
 passes, c2c forward and backward along y and z, in place."""
