@@ -91,7 +91,11 @@ __device__ __forceinline__ bool dispatch_n(const BatchDesc& D, Cx<T>* Sm, long l
 }
 
 // Four 256-thread CTAs per SM (at most 64 registers a thread): tiles are
-// short, so occupancy hides their load / exchange / store phases.
+// short, so occupancy hides their load / exchange / store phases.  The
+// kernel spills about 200 bytes a thread at 64 registers; the 64-grid
+// forward + backward batch still measured fastest so: 1.94 ms, against
+// 2.32 ms with three CTAs per SM (80 registers) and 3.15 ms with two (128,
+// no spills).
 template <typename T>
 __global__ void __launch_bounds__(kBT, 4)
     batch_kernel(const BatchDesc* __restrict__ desc, const long long* __restrict__ prefix, int ndesc,
