@@ -92,31 +92,45 @@ __device__ __forceinline__ bool dispatch_n(const BatchDesc& D, Cx<T>* Sm, long l
 
 // Four 256-thread CTAs per SM (at most 64 registers a thread): tiles are
 // short, so occupancy hides their load / exchange / store phases.  The
-// kernel spills about 200 bytes a thread at 64 registers; the 64-grid
-// forward + backward batch still measured fastest so: 1.94 ms, against
-// 2.32 ms with three CTAs per SM (80 registers) and 3.15 ms with two (128,
-// no spills).
+// kernel spills a few hundred bytes a thread at 64 registers; the 64-grid
+// forward + backward batch still measured fastest so (with one ticket a
+// tile and no look-ahead: 1.94 ms, against 2.32 ms with three CTAs per SM,
+// 80 registers, and 3.15 ms with two, 128 registers and no spills).
 template <typename T>
 __global__ void __launch_bounds__(kBT, 4)
     batch_kernel(const BatchDesc* __restrict__ desc, const long long* __restrict__ prefix, int ndesc,
                  int* sync) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ long long s_ticket;
+  __shared__ unsigned int s_ticket;
   Cx<T>* Sm = reinterpret_cast<Cx<T>*>(smem_raw);
-  const long long total = prefix[ndesc];
+  // Thread 0 claims each ticket one tile ahead (the atomic's latency then
+  // overlaps a tile), and signals a tile's completion at the start of the
+  // next one, while the other warps already load it.  A CTA's tickets only
+  // grow, so its descriptor index only moves forward.  The wait stays
+  // deadlock-free: the smallest unfinished ticket is always one a CTA is
+  // running (a CTA holds its claimed ticket only behind a smaller one), and
+  // a CTA signals its last tile before it waits for anything.
+  unsigned int next = 0;
+  if (threadIdx.x == 0) next = atomicAdd(reinterpret_cast<unsigned int*>(sync), 1u);
+  int lo = -1;  // descriptor of the previous tile (-1: none yet)
   for (;;) {
+    if (threadIdx.x == 0) s_ticket = next;
+    // every thread's stores of the previous tile, and its reads of the
+    // shared tile, come before this barrier
     __syncthreads();
-    if (threadIdx.x == 0) s_ticket = (long long)atomicAdd(reinterpret_cast<unsigned int*>(sync), 1u);
-    __syncthreads();
-    const long long tk = s_ticket;
-    if (tk >= total) break;
-    // descriptor i with prefix[i] <= tk < prefix[i + 1]
-    int lo = 0, hi = ndesc - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) / 2;
-      if (prefix[mid] <= tk) lo = mid;
-      else hi = mid - 1;
+    const long long tk = (long long)s_ticket;
+    const bool more = tk < __ldg(prefix + ndesc);
+    if (threadIdx.x == 0) {
+      if (lo >= 0) {
+        __threadfence();  // cumulative through the barrier: the whole CTA's stores
+        atomicAdd(sync + 2 + lo, 1);
+      }
+      if (more) next = atomicAdd(reinterpret_cast<unsigned int*>(sync), 1u);
     }
+    if (!more) break;
+    // descriptor i with prefix[i] <= tk < prefix[i + 1]
+    if (lo < 0) lo = 0;
+    while (__ldg(prefix + lo + 1) <= tk) ++lo;
     const BatchDesc& D = desc[lo];
     const long long tile = tk - prefix[lo];
     if (D.dep >= 0) {
@@ -134,9 +148,6 @@ __global__ void __launch_bounds__(kBT, 4)
       default: ok = dispatch_n<T, K_C2R, false>(D, Sm, tile); break;
     }
     if (!ok && threadIdx.x == 0) atomicExch(sync + 1, 2);
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(sync + 2 + lo, 1);
   }
 }
 
