@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(kMaxThreads)
     axis_pass_kernel(const __grid_constant__ PassArgs a) {
   using C = Cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  chained_entry();
   LineCtx<T, KIND, CONTIG> c;
   c.init(a);
   const size_t e = (size_t)a.n * a.L;
@@ -111,9 +112,9 @@ cudaError_t launch_typed(const PassArgs& a, cudaStream_t stream) {
   }
   const dim3 block = CONTIG ? dim3(a.tpl, a.L) : dim3(a.L, a.tpl);
   const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
-  kern<<<grid, block, smem, stream>>>(a);
+  const cudaError_t err = launch_chained(kern, grid, block, smem, stream, a);
   g_launches.fetch_add(1, std::memory_order_relaxed);
-  return cudaGetLastError();
+  return err != cudaSuccess ? err : cudaGetLastError();
 }
 
 // Identity copy, 16 bytes per access, 4 accesses in flight per thread.

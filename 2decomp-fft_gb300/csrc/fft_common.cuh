@@ -722,5 +722,45 @@ struct LineCtx {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Chained launches of the axis passes (programmatic dependent launch).
+// ---------------------------------------------------------------------------
+// A pass launched with launch_chained may start while the previous kernel of
+// its stream finishes.  Its first action is chained_entry(): wait until that
+// kernel has completed and its memory is visible (a no-op for a kernel
+// launched without the attribute), then let the next chained pass begin to
+// launch.  Every CTA of this grid is then resident or done, so the next
+// grid's waiting CTAs cannot keep any of them from running.
+__device__ __forceinline__ void chained_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 }  // namespace dev
+
+// Launch of an axis-pass kernel that overlaps its launch with the end of the
+// previous kernel in the stream; the kernel must call dev::chained_entry()
+// before it touches global memory.  Measured on GB300: stream launches of
+// small grids gain 5-25 % (256^3 FP32 round trip 0.142 -> 0.128 ms, 384
+// per-grid launches 2.79 -> 2.12 ms), while the same launches replayed from
+// a CUDA graph got slower (1.85 -> 2.03 ms), so a launch into a stream that
+// is being captured stays a plain one.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_chained(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                           Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &capture) != cudaSuccess) capture = cudaStreamCaptureStatusActive;
+  cfg.attrs = attr;
+  cfg.numAttrs = capture == cudaStreamCaptureStatusNone ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
+}
+
 }  // namespace gbfft

@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(fast_max_threads(E, sizeof(T)), 1)
     fast_pass_kernel(const __grid_constant__ PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* Sm = reinterpret_cast<Cx<T>*>(smem_raw);
+  chained_entry();
   // launched in clusters: start together, so that neighbouring CTAs' loads
   // of the same rows are in the DRAM queues at the same time
   if (a.csync) cooperative_groups::this_cluster().sync();
@@ -239,9 +240,9 @@ cudaError_t launch_ne(const PassArgs& a, cudaStream_t stream) {
   }
   if (a.csync) return cudaErrorInvalidValue;  // a cluster barrier needs a cluster launch
   const dim3 grid((unsigned)tiles, CONTIG ? 1u : (unsigned)a.nv);
-  kern<<<grid, block, smem, stream>>>(a);
+  const cudaError_t err = launch_chained(kern, grid, block, smem, stream, a);
   add_launches(1);
-  return cudaGetLastError();
+  return err != cudaSuccess ? err : cudaGetLastError();
 }
 
 // Lines of 512 and 1024 points have two plans: 32 points a thread (two

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(gen_max_threads(PlanOf<N>::type::E, sizeof(T))
   using P = typename PlanOf<N>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* Sm = reinterpret_cast<Cx<T>*>(smem_raw);
+  chained_entry();
   LineCtx<T, KIND, CONTIG> c;
   c.init(a);
   Cx<T> v[P::E];
@@ -49,9 +50,9 @@ cudaError_t launch_n(const PassArgs& a, cudaStream_t stream) {
   }
   const dim3 block = CONTIG ? dim3(P::TPL, a.L) : dim3(a.L, P::TPL);
   const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
-  kern<<<grid, block, smem, stream>>>(a);
+  const cudaError_t err = launch_chained(kern, grid, block, smem, stream, a);
   add_launches(1);
-  return cudaGetLastError();
+  return err != cudaSuccess ? err : cudaGetLastError();
 }
 
 template <typename T, int KIND, bool CONTIG>

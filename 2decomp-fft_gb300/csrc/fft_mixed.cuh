@@ -73,6 +73,7 @@ template <typename T, int KIND, bool CONTIG, int N>
 __global__ void __launch_bounds__(256) mixed_pass_kernel(const __grid_constant__ PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* Sm = reinterpret_cast<Cx<T>*>(smem_raw);
+  chained_entry();
   LineCtx<T, KIND, CONTIG> c;
   c.init(a);
   run_mixed<N>(c, Sm);
@@ -89,9 +90,9 @@ cudaError_t launch_n(const PassArgs& a, cudaStream_t stream) {
   }
   const dim3 block = CONTIG ? dim3(TPL, a.L) : dim3(a.L, TPL);
   const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L), CONTIG ? 1u : (unsigned)a.nv);
-  kern<<<grid, block, smem, stream>>>(a);
+  const cudaError_t err = launch_chained(kern, grid, block, smem, stream, a);
   add_launches(1);
-  return cudaGetLastError();
+  return err != cudaSuccess ? err : cudaGetLastError();
 }
 
 #define GBFFT_MIXED_CASES(T, KIND, CONTIG)                 \
