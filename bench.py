@@ -636,14 +636,18 @@ def run_gb300(args):
     yh = hb.empty(x.shape, x.dtype)
     xd = torch.empty_like(x)
     e2e_steps = max(3, min(args.steps, 20))
-    # On these machines the host link can stay slow in both directions at
-    # once (one-way copies at full speed) for a minute or more after other
-    # processes freed large amounts of memory.  Wait, at most 90 s, until a
-    # short link test shows healthy concurrent traffic; the wait and the link
+    # On these machines the host link can run at a fraction of its rate in
+    # one direction, or in both at once, for a minute or more after other
+    # work on the machine (the other direction at full speed).  Wait, at most
+    # 90 s, until no reading of a short link test (each direction alone, both
+    # at once) is below 60 % of the faster direction; the wait and the link
     # state are reported with the figure.
+    def link_degraded(lk):
+        return min(lk["h2d"], lk["d2h"], lk["both_each"]) < 0.6 * max(lk["h2d"], lk["d2h"])
+
     link = link_gbs(xh, xd, stream, host2=yh)
     t_settle = time.time()
-    while (link["both_each"] < 0.75 * min(link["h2d"], link["d2h"]) and time.time() - t_settle < 90.0):
+    while link_degraded(link) and time.time() - t_settle < 90.0:
         time.sleep(2.0)
         link = link_gbs(xh, xd, stream, reps=2, host2=yh)
     settle_s = round(time.time() - t_settle, 1)
