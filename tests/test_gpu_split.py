@@ -111,3 +111,22 @@ def test_split_and_plain_agree_closely():
     assert d <= TOL
     p.close()
     q.close()
+
+
+@pytest.mark.parametrize("fmt,shape", [(1, (256, 48, 27)), (3, (96, 50, 512)), (1, (48, 40, 27))])
+def test_split_on_non_power_of_two_axes(fmt, shape):
+    # only the 256-, 512- and 1024-point axes have split stages; the other
+    # axes of the same engine run the plain FP32 kernels (a grid with none,
+    # like 48 x 40 x 27, is the plain form throughout)
+    nx, ny, nz = shape
+    x = np.random.default_rng(17).uniform(-1, 1, (nz, ny, nx))
+    e = split_engine(fmt, nx, ny, nz)
+    xd = torch.from_numpy(x.astype(np.float32)).cuda()
+    s = e.empty_spectral()
+    e.r2c(xd, s)
+    assert rel(s.cpu().numpy(), O.fft3d_r2c(x, fmt)) <= TOL
+    y = e.empty_physical()
+    e.c2r(s, y)
+    assert rel(y.cpu().numpy() / (nx * ny * nz), x) <= TOL
+    e.status()
+    e.close()
