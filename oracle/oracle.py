@@ -17,7 +17,6 @@ exact transpose chain of examples/test2d) and cross-checked with pocketfft;
 the Fortran reference itself cannot be compiled here.
 """
 import ctypes
-import os
 
 import numpy as np
 

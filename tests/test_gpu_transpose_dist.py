@@ -8,8 +8,6 @@ GPU.  Each send buffer must equal the oracle's restated mem_split bit for
 bit, and each rank's pencil after x -> y -> z -> y -> x must equal its slice
 of the global array (the reference's test2d chain).  Blocks that would reach
 past a buffer are rejected before any launch."""
-import ctypes
-
 import numpy as np
 import pytest
 

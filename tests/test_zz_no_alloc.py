@@ -10,7 +10,6 @@ passes on its own in a fresh process (the first call does the per-device
 set-up).  Tolerances are those of the parity tests: relative L2 <= 1e-12 in
 double, <= 2e-6 in single.
 """
-import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
