@@ -1464,19 +1464,14 @@ int gbfft_engine_set_tile(gbfft_engine_t e, int kind, int lines) {
     return GBFFT_OK;
   }
   const bool fast = fast_length(p.n);
-  const bool contig_pass = (kind == GBFFT_PASS_C2C_X) ||
-                           ((kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R) &&
-                            e->format == GBFFT_PHYSICAL_IN_X);
+  const bool contiguous = (kind == GBFFT_PASS_C2C_X) ||
+                          ((kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R) &&
+                           e->format == GBFFT_PHYSICAL_IN_X);
   const int fe = p.fast_e;
   int tpl = fast ? p.n / fe : p.tpl;
   const int maxt = fast ? fast_max_threads(fe, e->prec) : kMaxThreads;
-  if (!fast) {
-    const bool contiguous = (kind == GBFFT_PASS_C2C_X) ||
-                            ((kind == GBFFT_PASS_R2C || kind == GBFFT_PASS_C2R) &&
-                             e->format == GBFFT_PHYSICAL_IN_X);
-    if (!contiguous)
-      while (lines * tpl > kMaxThreads && tpl > 32) tpl /= 2;
-  }
+  if (!fast && !contiguous)
+    while (lines * tpl > kMaxThreads && tpl > 32) tpl /= 2;
   if (lines * tpl > maxt) return fail(GBFFT_ERR_INVALID, "tile exceeds the kernel's thread limit");
   const size_t smem = fast ? (size_t)fast_smem_entries(p.n, lines) * 2 * (size_t)e->prec
                             : pass_smem_bytes(e->prec, p.n, lines);
