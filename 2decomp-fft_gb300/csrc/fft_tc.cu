@@ -32,8 +32,9 @@
 // rows 16q..16q+15 in lanes 32q..32q+15), exchanges re / im between lane
 // pairs, twiddles and writes the stage-B operand; stage B likewise, its
 // results to a padded output tile and from there to global memory.  Every
-// mbarrier wait is bounded; a CTA that gives up sets the pass's status word
-// and stops (the decision is taken by the whole CTA).
+// mbarrier wait is bounded; a CTA that gives up sets the pass's status word,
+// waits (bounded) once more for the MMAs it committed, frees its TMEM and
+// stops (the decision is taken by the whole CTA).
 //
 // The DFT matrices and the twiddles come from the axis's n-root table
 // exp(-2 pi i m / N).
@@ -297,7 +298,12 @@ __global__ void __launch_bounds__(kThreads, 2) tc_pass_kernel(const __grid_const
       const bool got = t == 0 ? mbar_wait(bar_a, phase) : true;
       if (__syncthreads_or(!got)) {
         ok = false;
-        if (t == 0 && a.status) atomicExch(a.status, 1);
+        if (t == 0) {
+          if (a.status) atomicExch(a.status, 1);
+          // the MMAs this CTA committed may still be writing TMEM: give them
+          // a second bounded wait before the columns are freed below
+          mbar_wait(bar_a, phase);
+        }
         break;
       }
       phase ^= 1;
