@@ -110,3 +110,24 @@ def test_module_mirror_state_errors():
         assert main["xst"] == (1, 1, 1) and main["zsz"] == (8, 8, 8)
     finally:
         L.d2d_decomp_2d_finalize()
+
+
+def test_missing_library_fails_loudly():
+    # no silent fallback: without the built library the binding refuses to load
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, %r); import gbfft\n"
+            "try:\n    gbfft.lib()\nexcept ImportError as e:\n    print('refused:', e)\n    raise SystemExit(3)\n"
+            % os.path.join(ROOT, "2decomp-fft_gb300"))
+    env = dict(os.environ, GBFFT_LIBRARY=os.path.join(ROOT, "no_such_dir", "libgbfft.so"))
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 3 and "refused: libgbfft.so is not built" in r.stdout
+
+
+@pytest.mark.skipif(__import__("torch").cuda.is_available(), reason="a GPU is present")
+def test_engine_without_a_gpu_is_an_error_not_a_fallback():
+    # the library has no CPU path: engine creation needs the device and
+    # reports why it cannot have it
+    with pytest.raises(gbfft.GbfftError) as ei:
+        gbfft.Engine(1, 16, 16, 16, prec=gbfft.PREC_SINGLE)
+    assert "cuda" in str(ei.value).lower()
