@@ -2,7 +2,7 @@
 (gbfft_box_copy) through the C ABI.  Every rank of the grid runs in its own
 host thread of this one process (one GPU; the device work of all threads is
 ordered on the default stream, no kernel waits for another), exchanging its
-slabs through an in-process mailbox in the driver's batches; each rank's
+slabs through an in-process mailbox in update_halo's message batches; each rank's
 halo-extended array must equal the oracle's (oracle/halo.py) on the cells
 the reference defines, bit for bit.  Boxes outside an array are rejected
 before any launch."""
